@@ -1,0 +1,131 @@
+/*
+ * gbivf -- GB300-native IVF-PQ search, C ABI.
+ *
+ * Drop-in for the IVF-PQ search path of rafaelms101/mestrado. Every entry
+ * point takes plain pointers and sizes, returns a status (GBIVF_OK or an
+ * error code; gbivf_last_error() gives the message of the calling thread's
+ * last failure) and never exits the process. Host-pointer entry points copy
+ * their inputs to the GPU, run, copy the results back and return when the
+ * results are in the caller's buffers. The caller owns every buffer; an
+ * index handle owns its device memory, so a process may hold many indexes.
+ *
+ * Conventions kept from the reference:
+ *   - index content: coarse centroids (C x d), nsq sub-quantizers of ks
+ *     centroids each (ks <= 256, so codes are bytes), one inverted list per
+ *     coarse centroid holding base ids and PQ codes;
+ *   - ids are 0-based row-major nq x k for ivfpq_search
+ *     (sequential/ivf_pq/ivf_search.cpp:133), 1-based column-major k x nq for
+ *     pq_search (sequential/pq-utils/pq_search.cpp:58-63), packed at
+ *     qid_to_starting_outid for core_gpu (parallel2/ivf_pq/ivf_search.cpp:
+ *     127-149);
+ *   - distances are squared L2 in the reference's float arithmetic.
+ * Where the reference cannot return k results it asserts (nn.c:468); here
+ * the missing slots are filled with id -1 and distance +inf.
+ */
+#ifndef GBIVF_H
+#define GBIVF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBIVF_OK 0
+#define GBIVF_ERR_INVALID 1     /* bad argument */
+#define GBIVF_ERR_CUDA 2        /* CUDA runtime error */
+#define GBIVF_ERR_NOMEM 3       /* device or host allocation failed */
+#define GBIVF_ERR_UNSUPPORTED 4 /* valid but outside what this build supports */
+
+/* search flags */
+#define GBIVF_RERANK 0x1u       /* exact L2 re-rank of the kl ADC candidates to k */
+#define GBIVF_TABLE_DIRECT 0x2u /* tables as sum (r-c)^2 (parallel2) instead of the expansion */
+
+typedef struct gbivf_index gbivf_index;
+
+const char *gbivf_last_error(void);
+int gbivf_version(void);
+
+/* Upload an IVF-PQ index (flat layout). coa: coarsek x d; pq: nsq x ks x
+ * (d/nsq), sub-quantizer s centroid c at pq[(s*ks + c)*(d/nsq)]; list l
+ * holds rows list_off[l] .. list_off[l+1]-1 of ids (int32) and codes
+ * (nsq bytes per row).
+ * Replaces: preallocate_gpu_mem(pqtipo, ivf_t*, int)
+ * (parallel2/ivf_pq/mycuda.h:8) and the ivfpq_t / ivf_t arguments of
+ * ivfpq_search (sequential/ivf_pq/ivf_search.h:20). */
+int gbivf_index_create(gbivf_index **out, int device, int d, int coarsek, const float *coa,
+                       int nsq, int ks, const float *pq, const int64_t *list_off,
+                       const int32_t *ids, const uint8_t *codes);
+
+/* Upload an index given as the reference holds it: ivfpq_t fields plus one
+ * ivf_t per list (ids, idstam, int32 codes n x nsq).
+ * pq_centroids[s] is the ks x ds array of sub-quantizer s (pqtipo.centroids,
+ * sequential/pq-utils/pq_new.h:26-33); list_ids[l] / list_codes[l] /
+ * list_sizes[l] are ivf[l].ids / ivf[l].codes.mat / ivf[l].idstam
+ * (sequential/ivf_pq/myIVF.h:23-27). Codes must be < ks <= 256.
+ * Replaces: preallocate_gpu_mem (parallel2/ivf_pq/mycuda.cu:193-221). */
+int gbivf_index_create_from_lists(gbivf_index **out, int device, int d, int coarsek,
+                                  const float *coa, int nsq, int ks,
+                                  const float *const *pq_centroids, const int32_t *list_sizes,
+                                  const int32_t *const *list_ids,
+                                  const int32_t *const *list_codes);
+
+/* Raw base vectors (n x d, row id = base id) for GBIVF_RERANK: the
+ * `mat vbase` argument of ivfpq_search (sequential/ivf_pq/ivf_search.cpp:9,
+ * 115-121), uploaded once instead of per call. */
+int gbivf_index_set_base(gbivf_index *ix, const float *base, int64_t n, int d);
+
+/* Replaces: deallocate_gpu_mem() (parallel2/ivf_pq/mycuda.h:9). */
+int gbivf_index_destroy(gbivf_index *ix);
+
+/* d, coarsek, nsq, ks, number of stored vectors (any pointer may be NULL). */
+int gbivf_index_dims(const gbivf_index *ix, int *d, int *coarsek, int *nsq, int *ks, int64_t *n);
+
+/* ivfpq_search(ivfpq, ivf, vquery, vbase, k, kl, w, ids, dis)
+ * (sequential/ivf_pq/ivf_search.cpp:9-153). queries: nq x d host floats.
+ * With GBIVF_RERANK: the kl best ADC candidates are re-ranked by exact L2
+ * against the base set with gbivf_index_set_base, keeping k (the reference
+ * always re-ranks). Without it: the k best ADC candidates (kl ignored).
+ * ids: nq x k (0-based base ids), dis: nq x k distances (the reference
+ * leaves dis unwritten; here it receives the re-rank or ADC distances). */
+int gbivf_ivfpq_search(gbivf_index *ix, const float *queries, int nq, int k, int kl, int w,
+                       unsigned flags, int32_t *ids, float *dis);
+
+/* Same, with device pointers, enqueued on `stream` (a cudaStream_t, NULL =
+ * the default stream); returns after launching. */
+int gbivf_ivfpq_search_device(gbivf_index *ix, const float *d_queries, int nq, int k, int kl,
+                              int w, unsigned flags, int32_t *d_ids, float *d_dis, void *stream);
+
+/* The coarse stage alone: knn_full(2, nq, C, d, w, coa, queries, ...)
+ * (sequential/ivf_pq/ivf_search.cpp:37-38): the w nearest lists per query,
+ * ascending. coaidx, coadis: nq x w host arrays. */
+int gbivf_coarse_assign(gbivf_index *ix, const float *queries, int nq, int w, int32_t *coaidx,
+                        float *coadis);
+
+/* core_gpu(PQ, residual, ivf, ivf_size, rid_to_ivf, qid_to_starting_outid,
+ * idxs, dists, k, w) (parallel2/ivf_pq/mycuda.cu:119-188): residual is
+ * nres x d (nres = nq*w), list rid_to_ivf[r] for residual r; tables are the
+ * direct sum of squared differences (mycuda.cu:59-64). For query q the
+ * min(k, sum of its lists' sizes) best (distance, base id) are written
+ * ascending at qid_to_starting_outid[q]. */
+int gbivf_core_gpu(gbivf_index *ix, const float *residual, int nres, const int32_t *rid_to_ivf,
+                   const int32_t *qid_to_starting_outid, int32_t *idxs, float *dists, int k,
+                   int w);
+
+/* Flat PQ: upload n codes (n x nsq bytes) with their quantizer.
+ * Replaces the codebook / pqtipo arguments of pq_search
+ * (sequential/pq-utils/pq_search.h:21). */
+int gbivf_pq_create(gbivf_index **out, int device, int d, int nsq, int ks, const float *pq,
+                    const uint8_t *codes, int64_t n);
+
+/* pq_search(pq, codebook, vquery, k, dis, ids)
+ * (sequential/pq-utils/pq_search.cpp:10-68): exhaustive ADC, k best per
+ * query; dis and ids are k x nq column-major, ids 1-based. k <= n. */
+int gbivf_pq_search(gbivf_index *ix, const float *queries, int nq, int k, float *dis,
+                    int32_t *ids);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBIVF_H */

@@ -1,0 +1,537 @@
+// C ABI of the GB300 IVF-PQ engine (declared in include/gbivf.h).
+//
+// Host side: validates arguments, lays the index out in HBM (list starts
+// aligned to 16 bytes so that code rows load as 4/8/16-byte vectors),
+// computes the index-constant norms once, keeps a per-index workspace that
+// grows on demand, and enqueues the kernels of kernels.cu.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/gbivf.h"
+#include "kernels.cuh"
+
+using namespace gbivf;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    g_err = b;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? GBIVF_ERR_NOMEM : GBIVF_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// growable device buffer
+struct DBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes + bytes / 4;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+// reference-order norms on the host (nn.c:129-145)
+float norm_f_host(const float* a, int d) {
+    float s = 0.0f;
+    for (int j = 0; j < d; j++) {
+        float p = a[j] * a[j];
+        s = s + p;
+    }
+    return s;
+}
+
+double norm_d_host(const float* a, int d) {
+    double s = 0.0;
+    for (int j = 0; j < d; j++) {
+        float p = a[j] * a[j];
+        s = s + (double)p;
+    }
+    return s;
+}
+
+}  // namespace
+
+struct gbivf_index {
+    int device = 0;
+    DevIndex dx;
+    std::vector<int32_t> h_len;  // list sizes (host copy)
+    int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
+    std::vector<void*> owned;    // index allocations
+    DBuf base, base_norm;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    // workspace
+    DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start;
+    std::vector<int32_t> h_tmp_ids;
+    std::vector<float> h_tmp_dis;
+};
+
+namespace {
+
+template <class T>
+cudaError_t upload(gbivf_index* ix, const T* h, size_t count, T** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    ix->owned.push_back(p);
+    if (count) e = cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+    *out = static_cast<T*>(p);
+    return e;
+}
+
+void free_index(gbivf_index* ix) {
+    for (void* p : ix->owned) cudaFree(p);
+    ix->owned.clear();
+    for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
+                    &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start})
+        b->release();
+    if (ix->stream) cudaStreamDestroy(ix->stream);
+    ix->stream = nullptr;
+}
+
+int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
+                const float* pq, const int64_t* list_off, const int32_t* ids, const uint8_t* codes) {
+    if (!out) return fail(GBIVF_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (d <= 0 || nsq <= 0 || d % nsq) return fail(GBIVF_ERR_INVALID, "d=%d must be a positive multiple of nsq=%d", d, nsq);
+    if (ks <= 0 || ks > 256) return fail(GBIVF_ERR_UNSUPPORTED, "ks=%d: codes are bytes, so ks must be in 1..256", ks);
+    if (coarsek <= 0) return fail(GBIVF_ERR_INVALID, "coarsek=%d", coarsek);
+    if (nsq * ks > 64 * 256) return fail(GBIVF_ERR_UNSUPPORTED, "nsq*ks=%d exceeds the shared-memory table limit", nsq * ks);
+    if (!coa || !pq || !list_off) return fail(GBIVF_ERR_INVALID, "NULL index array");
+    if (list_off[0] != 0) return fail(GBIVF_ERR_INVALID, "list_off[0] must be 0");
+    for (int l = 0; l < coarsek; l++)
+        if (list_off[l + 1] < list_off[l]) return fail(GBIVF_ERR_INVALID, "list_off decreases at list %d", l);
+    const int64_t n = list_off[coarsek];
+    if (n > 0 && (!ids || !codes)) return fail(GBIVF_ERR_INVALID, "NULL ids/codes");
+    for (int64_t i = 0; i < n * nsq; i++)
+        if (codes[i] >= ks) return fail(GBIVF_ERR_INVALID, "code %d >= ks=%d at byte %lld", codes[i], ks, (long long)i);
+    for (int l = 0; l < coarsek; l++)
+        if (list_off[l + 1] - list_off[l] > 0x7fffffffLL) return fail(GBIVF_ERR_UNSUPPORTED, "list %d too long", l);
+    if (n > 0xffffffffLL) return fail(GBIVF_ERR_UNSUPPORTED, "more than 2^32 vectors");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GBIVF_ERR_CUDA, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(GBIVF_ERR_INVALID, "device %d of %d", device, ndev);
+    DeviceGuard g(device);
+    if (!g.ok) return fail(GBIVF_ERR_CUDA, "cudaSetDevice(%d) failed", device);
+
+    auto* ix = new gbivf_index();
+    ix->device = device;
+    for (int64_t i = 0; i < n; i++) {
+        if (i == 0 || ids[i] < ix->min_id) ix->min_id = ids[i];
+        if (i == 0 || ids[i] > ix->max_id) ix->max_id = ids[i];
+    }
+    const int ds = d / nsq;
+    // list starts aligned so that a list's first code row sits on 16 bytes
+    int g16 = std::gcd(nsq, 16);
+    const int64_t align_rows = 16 / g16;
+    std::vector<int64_t> beg(coarsek);
+    ix->h_len.resize(coarsek);
+    int64_t rows = 0;
+    for (int l = 0; l < coarsek; l++) {
+        rows = (rows + align_rows - 1) / align_rows * align_rows;
+        beg[l] = rows;
+        ix->h_len[l] = (int32_t)(list_off[l + 1] - list_off[l]);
+        rows += ix->h_len[l];
+    }
+    rows = (rows + align_rows - 1) / align_rows * align_rows;
+    std::vector<uint8_t> pcodes((size_t)std::max<int64_t>(rows, 1) * nsq, 0);
+    std::vector<int32_t> pids((size_t)std::max<int64_t>(rows, 1), -1);
+    for (int l = 0; l < coarsek; l++) {
+        int64_t len = ix->h_len[l];
+        if (!len) continue;
+        memcpy(&pcodes[(size_t)beg[l] * nsq], codes + list_off[l] * nsq, (size_t)len * nsq);
+        memcpy(&pids[(size_t)beg[l]], ids + list_off[l], (size_t)len * sizeof(int32_t));
+    }
+    std::vector<float> cn(coarsek);
+    for (int c = 0; c < coarsek; c++) cn[c] = norm_f_host(coa + (int64_t)c * d, d);
+    std::vector<double> pn((size_t)nsq * ks);
+    for (int e = 0; e < nsq * ks; e++) pn[e] = norm_d_host(pq + (int64_t)e * ds, ds);
+
+    DevIndex& dx = ix->dx;
+    dx.d = d;
+    dx.C = coarsek;
+    dx.m = nsq;
+    dx.ks = ks;
+    dx.ds = ds;
+    dx.rows = rows;
+    cudaError_t e = cudaSuccess;
+    float *p_coa, *p_cn, *p_pq;
+    double* p_pn;
+    int64_t* p_beg;
+    int32_t *p_len, *p_ids;
+    uint8_t* p_codes;
+    if ((e = upload(ix, coa, (size_t)coarsek * d, &p_coa)) != cudaSuccess ||
+        (e = upload(ix, cn.data(), cn.size(), &p_cn)) != cudaSuccess ||
+        (e = upload(ix, pq, (size_t)nsq * ks * ds, &p_pq)) != cudaSuccess ||
+        (e = upload(ix, pn.data(), pn.size(), &p_pn)) != cudaSuccess ||
+        (e = upload(ix, beg.data(), beg.size(), &p_beg)) != cudaSuccess ||
+        (e = upload(ix, ix->h_len.data(), ix->h_len.size(), &p_len)) != cudaSuccess ||
+        (e = upload(ix, pcodes.data(), pcodes.size(), &p_codes)) != cudaSuccess ||
+        (e = upload(ix, pids.data(), pids.size(), &p_ids)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        free_index(ix);
+        delete ix;
+        return cuda_fail(e, "index upload");
+    }
+    dx.coa = p_coa;
+    dx.coa_norm = p_cn;
+    dx.pq = p_pq;
+    dx.pq_norm = p_pn;
+    dx.list_beg = p_beg;
+    dx.list_len = p_len;
+    dx.codes = p_codes;
+    dx.ids = p_ids;
+    *out = ix;
+    return GBIVF_OK;
+}
+
+// queries per coarse-distance block: at most 64 Mi floats of scratch and
+// 65535 row tiles of 64 queries (the kernel's grid.y)
+int coarse_batch(int nq, int C) {
+    int64_t bq = std::min<int64_t>(nq, (64ll << 20) / C);
+    bq = std::min<int64_t>(bq, 65535ll * 64);
+    return (int)std::max<int64_t>(1, bq);
+}
+
+int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    if (k <= 0 || k > MAX_K) return fail(k <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "k=%d (1..%d)", k, MAX_K);
+    if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
+    if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
+    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if (flags & GBIVF_RERANK) {
+        if (kl <= 0 || kl > MAX_K) return fail(kl <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "kl=%d (1..%d)", kl, MAX_K);
+        if (!ix->base.p) return fail(GBIVF_ERR_INVALID, "GBIVF_RERANK needs gbivf_index_set_base first");
+        if (ix->max_id >= 0 && (ix->min_id < 0 || (int64_t)ix->max_id >= ix->dx.nbase))
+            return fail(GBIVF_ERR_INVALID, "stored ids %d..%d fall outside the %lld base rows", ix->min_id, ix->max_id,
+                        (long long)ix->dx.nbase);
+    }
+    return GBIVF_OK;
+}
+
+// queries already on the device; everything enqueued on st
+int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl, int w, unsigned flags,
+                       int32_t* d_ids, float* d_dis, cudaStream_t st) {
+    if (nq == 0) return GBIVF_OK;
+    const DevIndex& dx = ix->dx;
+    CK(ix->w_qn.ensure(sizeof(double) * nq));
+    CK(ix->w_coaidx.ensure(sizeof(int32_t) * (size_t)nq * w));
+    CK(ix->w_coadis.ensure(sizeof(float) * (size_t)nq * w));
+    double* qn = ix->w_qn.as<double>();
+    int32_t* coaidx = ix->w_coaidx.as<int32_t>();
+    float* coadis = ix->w_coadis.as<float>();
+    CK(launch_norm_d(d_q, nq, dx.d, qn, st));
+    if (dx.C == 1) {
+        CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
+    } else {
+        int bq = coarse_batch(nq, dx.C);
+        CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
+        float* cd = ix->w_cdist.as<float>();
+        for (int q0 = 0; q0 < nq; q0 += bq) {
+            int nb = std::min(bq, nq - q0);
+            CK(launch_coarse_dist(dx, d_q + (int64_t)q0 * dx.d, qn + q0, nb, cd, st));
+            CK(launch_coarse_select(cd, nb, dx.C, w, coaidx + (int64_t)q0 * w, coadis + (int64_t)q0 * w, st));
+        }
+    }
+    ScanArgs a;
+    a.nq = nq;
+    a.w = w;
+    a.k = k;
+    a.kl = kl;
+    a.flags = (flags & GBIVF_RERANK ? SCAN_RERANK : 0) | (flags & GBIVF_TABLE_DIRECT ? SCAN_TABLE_DIRECT : 0);
+    a.queries = d_q;
+    a.qnorm = qn;
+    a.probes = coaidx;
+    a.out_ids = d_ids;
+    a.out_dis = d_dis;
+    CK(launch_scan(dx, a, st));
+    return GBIVF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbivf_last_error(void) { return g_err.c_str(); }
+
+int gbivf_version(void) { return 1; }
+
+int gbivf_index_create(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
+                       const float* pq, const int64_t* list_off, const int32_t* ids, const uint8_t* codes) {
+    return create_impl(out, device, d, coarsek, coa, nsq, ks, pq, list_off, ids, codes);
+}
+
+int gbivf_index_create_from_lists(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq,
+                                  int ks, const float* const* pq_centroids, const int32_t* list_sizes,
+                                  const int32_t* const* list_ids, const int32_t* const* list_codes) {
+    if (!pq_centroids || !list_sizes || !list_ids || !list_codes) return fail(GBIVF_ERR_INVALID, "NULL argument");
+    if (d <= 0 || nsq <= 0 || d % nsq || coarsek <= 0) return fail(GBIVF_ERR_INVALID, "bad dimensions");
+    if (ks <= 0 || ks > 256) return fail(GBIVF_ERR_UNSUPPORTED, "ks=%d > 256 cannot be held as byte codes", ks);
+    const int ds = d / nsq;
+    std::vector<float> pq((size_t)nsq * ks * ds);
+    for (int s = 0; s < nsq; s++) {
+        if (!pq_centroids[s]) return fail(GBIVF_ERR_INVALID, "pq_centroids[%d] is NULL", s);
+        memcpy(&pq[(size_t)s * ks * ds], pq_centroids[s], sizeof(float) * ks * ds);
+    }
+    std::vector<int64_t> off(coarsek + 1, 0);
+    for (int l = 0; l < coarsek; l++) {
+        if (list_sizes[l] < 0) return fail(GBIVF_ERR_INVALID, "list %d size %d", l, list_sizes[l]);
+        off[l + 1] = off[l] + list_sizes[l];
+    }
+    std::vector<int32_t> ids((size_t)off[coarsek]);
+    std::vector<uint8_t> codes((size_t)off[coarsek] * nsq);
+    for (int l = 0; l < coarsek; l++) {
+        int n = list_sizes[l];
+        if (!n) continue;
+        if (!list_ids[l] || !list_codes[l]) return fail(GBIVF_ERR_INVALID, "list %d arrays are NULL", l);
+        memcpy(&ids[(size_t)off[l]], list_ids[l], sizeof(int32_t) * n);
+        for (int64_t i = 0; i < (int64_t)n * nsq; i++) {
+            int32_t c = list_codes[l][i];
+            if (c < 0 || c >= ks) return fail(GBIVF_ERR_INVALID, "list %d code %d outside 0..%d", l, c, ks - 1);
+            codes[(size_t)off[l] * nsq + i] = (uint8_t)c;
+        }
+    }
+    return create_impl(out, device, d, coarsek, coa, nsq, ks, pq.data(), off.data(), ids.data(), codes.data());
+}
+
+int gbivf_index_set_base(gbivf_index* ix, const float* base, int64_t n, int d) {
+    if (!ix || !base || n <= 0) return fail(GBIVF_ERR_INVALID, "bad base arguments");
+    if (d != ix->dx.d) return fail(GBIVF_ERR_INVALID, "base d=%d, index d=%d", d, ix->dx.d);
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    CK(ix->base.ensure(sizeof(float) * (size_t)n * d));
+    CK(ix->base_norm.ensure(sizeof(float) * (size_t)n));
+    CK(cudaMemcpyAsync(ix->base.p, base, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, ix->stream));
+    CK(launch_norm_f(ix->base.as<float>(), n, d, ix->base_norm.as<float>(), ix->stream));
+    CK(cudaStreamSynchronize(ix->stream));
+    ix->dx.base = ix->base.as<float>();
+    ix->dx.base_norm = ix->base_norm.as<float>();
+    ix->dx.nbase = n;
+    return GBIVF_OK;
+}
+
+int gbivf_index_destroy(gbivf_index* ix) {
+    if (!ix) return GBIVF_OK;
+    {
+        DeviceGuard g(ix->device);
+        if (ix->stream) cudaStreamSynchronize(ix->stream);
+        free_index(ix);
+    }
+    delete ix;
+    return GBIVF_OK;
+}
+
+int gbivf_index_dims(const gbivf_index* ix, int* d, int* coarsek, int* nsq, int* ks, int64_t* n) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (d) *d = ix->dx.d;
+    if (coarsek) *coarsek = ix->dx.C;
+    if (nsq) *nsq = ix->dx.m;
+    if (ks) *ks = ix->dx.ks;
+    if (n) {
+        int64_t s = 0;
+        for (int32_t v : ix->h_len) s += v;
+        *n = s;
+    }
+    return GBIVF_OK;
+}
+
+int gbivf_ivfpq_search_device(gbivf_index* ix, const float* d_queries, int nq, int k, int kl, int w,
+                              unsigned flags, int32_t* d_ids, float* d_dis, void* stream) {
+    int rc = check_search(ix, nq, k, kl, w, flags);
+    if (rc) return rc;
+    if (nq > 0 && (!d_queries || !d_ids || !d_dis)) return fail(GBIVF_ERR_INVALID, "NULL device buffer");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    return search_device_impl(ix, d_queries, nq, k, kl, w, flags, d_ids, d_dis, (cudaStream_t)stream);
+}
+
+int gbivf_ivfpq_search(gbivf_index* ix, const float* queries, int nq, int k, int kl, int w, unsigned flags,
+                       int32_t* ids, float* dis) {
+    int rc = check_search(ix, nq, k, kl, w, flags);
+    if (rc) return rc;
+    if (nq == 0) return GBIVF_OK;
+    if (!queries || !ids || !dis) return fail(GBIVF_ERR_INVALID, "NULL host buffer");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const size_t qb = sizeof(float) * (size_t)nq * ix->dx.d, ob = (size_t)nq * k;
+    CK(ix->w_q.ensure(qb));
+    CK(ix->w_ids.ensure(sizeof(int32_t) * ob));
+    CK(ix->w_dis.ensure(sizeof(float) * ob));
+    CK(cudaMemcpyAsync(ix->w_q.p, queries, qb, cudaMemcpyHostToDevice, ix->stream));
+    rc = search_device_impl(ix, ix->w_q.as<float>(), nq, k, kl, w, flags, ix->w_ids.as<int32_t>(),
+                            ix->w_dis.as<float>(), ix->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ids, ix->w_ids.p, sizeof(int32_t) * ob, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaMemcpyAsync(dis, ix->w_dis.p, sizeof(float) * ob, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaStreamSynchronize(ix->stream));
+    return GBIVF_OK;
+}
+
+int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, int32_t* coaidx, float* coadis) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
+    if (nq <= 0) return nq == 0 ? GBIVF_OK : fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    if (!queries || !coaidx || !coadis) return fail(GBIVF_ERR_INVALID, "NULL host buffer");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const DevIndex& dx = ix->dx;
+    const size_t qb = sizeof(float) * (size_t)nq * dx.d;
+    CK(ix->w_q.ensure(qb));
+    CK(ix->w_qn.ensure(sizeof(double) * nq));
+    CK(ix->w_coaidx.ensure(sizeof(int32_t) * (size_t)nq * w));
+    CK(ix->w_coadis.ensure(sizeof(float) * (size_t)nq * w));
+    CK(cudaMemcpyAsync(ix->w_q.p, queries, qb, cudaMemcpyHostToDevice, ix->stream));
+    CK(launch_norm_d(ix->w_q.as<float>(), nq, dx.d, ix->w_qn.as<double>(), ix->stream));
+    int bq = coarse_batch(nq, dx.C);
+    CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
+    for (int q0 = 0; q0 < nq; q0 += bq) {
+        int nb = std::min(bq, nq - q0);
+        CK(launch_coarse_dist(dx, ix->w_q.as<float>() + (int64_t)q0 * dx.d, ix->w_qn.as<double>() + q0, nb,
+                              ix->w_cdist.as<float>(), ix->stream));
+        CK(launch_coarse_select(ix->w_cdist.as<float>(), nb, dx.C, w, ix->w_coaidx.as<int32_t>() + (int64_t)q0 * w,
+                                ix->w_coadis.as<float>() + (int64_t)q0 * w, ix->stream));
+    }
+    CK(cudaMemcpyAsync(coaidx, ix->w_coaidx.p, sizeof(int32_t) * (size_t)nq * w, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaMemcpyAsync(coadis, ix->w_coadis.p, sizeof(float) * (size_t)nq * w, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaStreamSynchronize(ix->stream));
+    return GBIVF_OK;
+}
+
+int gbivf_core_gpu(gbivf_index* ix, const float* residual, int nres, const int32_t* rid_to_ivf,
+                   const int32_t* qid_to_starting_outid, int32_t* idxs, float* dists, int k, int w) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (w <= 0 || w > MAX_W || k <= 0 || k > MAX_K || nres < 0 || nres % w)
+        return fail(GBIVF_ERR_INVALID, "bad sizes nres=%d w=%d k=%d", nres, w, k);
+    if (nres == 0) return GBIVF_OK;
+    if (!residual || !rid_to_ivf || !qid_to_starting_outid || !idxs || !dists)
+        return fail(GBIVF_ERR_INVALID, "NULL host buffer");
+    const int nq = nres / w;
+    int64_t nout = 0;
+    for (int q = 0; q < nq; q++) {
+        int64_t L = 0;
+        for (int j = 0; j < w; j++) {
+            int l = rid_to_ivf[(int64_t)q * w + j];
+            if (l < 0 || l >= ix->dx.C) return fail(GBIVF_ERR_INVALID, "rid_to_ivf[%d]=%d", q * w + j, l);
+            L += ix->h_len[l];
+        }
+        if (qid_to_starting_outid[q] < 0) return fail(GBIVF_ERR_INVALID, "negative output offset");
+        nout = std::max<int64_t>(nout, qid_to_starting_outid[q] + std::min<int64_t>(L, k));
+    }
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const DevIndex& dx = ix->dx;
+    CK(ix->w_res.ensure(sizeof(float) * (size_t)nres * dx.d));
+    CK(ix->w_coaidx.ensure(sizeof(int32_t) * (size_t)nres));
+    CK(ix->w_start.ensure(sizeof(int32_t) * (size_t)nq));
+    CK(ix->w_ids.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nout, 1)));
+    CK(ix->w_dis.ensure(sizeof(float) * (size_t)std::max<int64_t>(nout, 1)));
+    CK(cudaMemcpyAsync(ix->w_res.p, residual, sizeof(float) * (size_t)nres * dx.d, cudaMemcpyHostToDevice, ix->stream));
+    CK(cudaMemcpyAsync(ix->w_coaidx.p, rid_to_ivf, sizeof(int32_t) * (size_t)nres, cudaMemcpyHostToDevice, ix->stream));
+    CK(cudaMemcpyAsync(ix->w_start.p, qid_to_starting_outid, sizeof(int32_t) * (size_t)nq, cudaMemcpyHostToDevice,
+                       ix->stream));
+    ScanArgs a;
+    a.nq = nq;
+    a.w = w;
+    a.k = k;
+    a.kl = k;
+    a.flags = SCAN_SRC_RESIDUAL | SCAN_TABLE_DIRECT | SCAN_OUT_PACKED;
+    a.residual = ix->w_res.as<float>();
+    a.probes = ix->w_coaidx.as<int32_t>();
+    a.out_start = ix->w_start.as<int32_t>();
+    a.out_ids = ix->w_ids.as<int32_t>();
+    a.out_dis = ix->w_dis.as<float>();
+    CK(launch_scan(dx, a, ix->stream));
+    // copy back only the written ranges
+    for (int q = 0; q < nq; q++) {
+        int64_t L = 0;
+        for (int j = 0; j < w; j++) L += ix->h_len[rid_to_ivf[(int64_t)q * w + j]];
+        int64_t cnt = std::min<int64_t>(L, k), o = qid_to_starting_outid[q];
+        if (!cnt) continue;
+        CK(cudaMemcpyAsync(idxs + o, ix->w_ids.as<int32_t>() + o, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, ix->stream));
+        CK(cudaMemcpyAsync(dists + o, ix->w_dis.as<float>() + o, sizeof(float) * cnt, cudaMemcpyDeviceToHost, ix->stream));
+    }
+    CK(cudaStreamSynchronize(ix->stream));
+    return GBIVF_OK;
+}
+
+int gbivf_pq_create(gbivf_index** out, int device, int d, int nsq, int ks, const float* pq, const uint8_t* codes,
+                    int64_t n) {
+    if (n < 0) return fail(GBIVF_ERR_INVALID, "n=%lld", (long long)n);
+    if (n > 0x7fffffffLL) return fail(GBIVF_ERR_UNSUPPORTED, "flat PQ limited to 2^31-1 codes");
+    if (d <= 0) return fail(GBIVF_ERR_INVALID, "d=%d", d);
+    std::vector<float> zero((size_t)d, 0.0f);
+    int64_t off[2] = {0, n};
+    std::vector<int32_t> ids((size_t)n);
+    for (int64_t i = 0; i < n; i++) ids[(size_t)i] = (int32_t)i;
+    return create_impl(out, device, d, 1, zero.data(), nsq, ks, pq, off, ids.data(), codes);
+}
+
+int gbivf_pq_search(gbivf_index* ix, const float* queries, int nq, int k, float* dis, int32_t* ids) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (ix->dx.C != 1) return fail(GBIVF_ERR_INVALID, "not a flat PQ index (use gbivf_pq_create)");
+    if (k > ix->h_len[0]) return fail(GBIVF_ERR_INVALID, "k=%d > n=%d (pq_search needs k <= n)", k, ix->h_len[0]);
+    if (nq <= 0) return nq == 0 ? GBIVF_OK : fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    std::vector<int32_t> rid((size_t)nq * k);
+    std::vector<float> rdis((size_t)nq * k);
+    int rc = gbivf_ivfpq_search(ix, queries, nq, k, 0, 1, 0u, rid.data(), rdis.data());
+    if (rc) return rc;
+    for (int q = 0; q < nq; q++)
+        for (int l = 0; l < k; l++) {  // column-major, 1-based
+            dis[(int64_t)nq * l + q] = rdis[(size_t)q * k + l];
+            ids[(int64_t)nq * l + q] = rid[(size_t)q * k + l] + 1;
+        }
+    return GBIVF_OK;
+}
+
+}  // extern "C"

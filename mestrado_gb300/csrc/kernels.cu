@@ -1,0 +1,406 @@
+// GB300 (sm_103a) kernels of the plain FP32 IVF-PQ search path.
+//
+// Reference path (rafaelms101/mestrado, sequential/ivf_pq/ivf_search.cpp:9-203):
+//   knn_full (coarse, k = w)           -> coarse_dist_kernel + coarse_select_kernel
+//   bsxfunMINUS + compute_cross_distances (m x ks tables)
+//   + sumidxtab2 (ADC) + k_min (kl)     -> ivf_scan_kernel (fused, one CTA per query)
+//   RERANK knn_full over kl candidates  -> tail of ivf_scan_kernel
+// and parallel2's core_gpu (parallel2/ivf_pq/mycuda.cu:28-188) through the
+// SCAN_SRC_RESIDUAL | SCAN_TABLE_DIRECT | SCAN_OUT_PACKED mode.
+//
+// All arithmetic mirrors the reference rounding (see common.cuh); ties are
+// broken by (distance, payload) keys (block_topk.cuh).
+#include <algorithm>
+
+#include "block_topk.cuh"
+#include "kernels.cuh"
+
+namespace gbivf {
+
+// ---------------------------------------------------------------------------
+// norms
+// ---------------------------------------------------------------------------
+
+__global__ void norm_d_kernel(const float* __restrict__ x, int64_t n, int d, double* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = x + i * d;
+    double s = 0.0;
+    for (int l = 0; l < d; l++) s = __dadd_rn(s, (double)__fmul_rn(r[l], r[l]));
+    out[i] = s;
+}
+
+__global__ void norm_f_kernel(const float* __restrict__ x, int64_t n, int d, float* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = norm_f_seq(x + i * d, d);
+}
+
+cudaError_t launch_norm_d(const float* x, int64_t n, int d, double* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    norm_d_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(x, n, d, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_f(const float* x, int64_t n, int d, float* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    norm_f_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(x, n, d, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// coarse distances: 64 x 64 output tile per CTA, 4 x 4 per thread, K chunks
+// of 32 staged in shared memory. Every output is one sequential dot product
+// over l = 0..d-1 (the netlib sgemm order), then the expansion epilogue.
+// ---------------------------------------------------------------------------
+
+constexpr int CD_TILE = 64, CD_K = 32;
+
+__global__ void __launch_bounds__(256) coarse_dist_kernel(
+    const float* __restrict__ X, int nq, const float* __restrict__ Cc, int C, int d,
+    const double* __restrict__ qnorm, const float* __restrict__ cnorm, float* __restrict__ out) {
+    __shared__ float Xs[CD_K][CD_TILE + 1];
+    __shared__ float Cs[CD_K][CD_TILE + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int q0 = blockIdx.y * CD_TILE, c0 = blockIdx.x * CD_TILE;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+
+    for (int l0 = 0; l0 < d; l0 += CD_K) {
+        for (int e = tid; e < CD_TILE * CD_K; e += 256) {
+            int row = e / CD_K, col = e % CD_K;
+            int l = l0 + col;
+            int qr = q0 + row, cr = c0 + row;
+            Xs[col][row] = (qr < nq && l < d) ? X[(int64_t)qr * d + l] : 0.0f;
+            Cs[col][row] = (cr < C && l < d) ? Cc[(int64_t)cr * d + l] : 0.0f;
+        }
+        __syncthreads();
+        const int lmax = min(CD_K, d - l0);
+        for (int l = 0; l < lmax; l++) {
+            float a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = Xs[l][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) b[j] = Cs[l][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(b[j], a[i]));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int q = q0 + ty + 16 * i;
+        if (q >= nq) continue;
+        double qn = qnorm[q];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int c = c0 + tx + 16 * j;
+            if (c < C) out[(int64_t)q * C + c] = expansion_from(qn, cnorm[c], acc[i][j]);
+        }
+    }
+}
+
+cudaError_t launch_coarse_dist(const DevIndex& ix, const float* q, const double* qnorm, int nq,
+                               float* out, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    dim3 grid((ix.C + CD_TILE - 1) / CD_TILE, (nq + CD_TILE - 1) / CD_TILE);
+    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// coarse k-min: one CTA per query over its row of C distances
+// ---------------------------------------------------------------------------
+
+constexpr int CS_NT = 128, CS_ITEMS = 8;
+
+static int pow2_at_least(int x) {
+    int n = 1;
+    while (n < x) n <<= 1;
+    return n;
+}
+
+__global__ void __launch_bounds__(CS_NT) coarse_select_kernel(
+    const float* __restrict__ dist, int C, int w, int kcap, int bcap,
+    int32_t* __restrict__ coaidx, float* __restrict__ coadis) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* best = reinterpret_cast<u64*>(smem);
+    u64* tmp = best + kcap;
+    u64* buf = tmp + kcap;
+    u64* thresh = buf + bcap;
+    int* cnt = reinterpret_cast<int*>(thresh + 1);
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap};
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const float* row = dist + (int64_t)q * C;
+    topk_init(s, w);
+    for (int i0 = 0; i0 < C; i0 += CS_NT * CS_ITEMS) {
+#pragma unroll
+        for (int it = 0; it < CS_ITEMS; it++) {
+            int c = i0 + it * CS_NT + tid;
+            bool valid = c < C;
+            float v = valid ? row[c] : 0.0f;
+            topk_offer(s, make_key(v, (uint32_t)c), valid);
+        }
+        topk_round_end(s, CS_NT * CS_ITEMS);
+    }
+    topk_finish(s);
+    const int nb = *s.nbest;
+    for (int j = tid; j < w; j += CS_NT) {
+        coaidx[(int64_t)q * w + j] = j < nb ? (int32_t)key_payload(best[j]) : -1;
+        coadis[(int64_t)q * w + j] = j < nb ? key_dist(best[j]) : __int_as_float(0x7f800000);
+    }
+}
+
+cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_t* coaidx,
+                                 float* coadis, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    int kcap = pow2_at_least(std::max(w, 2));
+    int bcap = pow2_at_least(std::max(2 * CS_NT * CS_ITEMS, kcap));
+    size_t sm = sizeof(u64) * (2 * kcap + bcap + 1) + 2 * sizeof(int);
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(coarse_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    coarse_select_kernel<<<nq, CS_NT, sm, st>>>(dist, C, w, kcap, bcap, coaidx, coadis);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// fused scan: per query (one CTA), for each probed list: residual, m x ks
+// table in shared memory, ADC over the list's codes, streaming top-k; then
+// the optional exact re-rank of the kl best.
+// ---------------------------------------------------------------------------
+
+constexpr int SC_NT = 256, SC_ITEMS = 4;
+
+struct ScanSmem {
+    size_t off_best, off_tmp, off_buf, off_thresh, off_table, off_xq, off_r, off_rn, off_prefix,
+        off_plist, off_cand, off_cnt, total;
+};
+
+static ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap) {
+    ScanSmem L;
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t align) {
+        o = (o + align - 1) / align * align;
+        size_t r = o;
+        o += bytes;
+        return r;
+    };
+    L.off_best = take(sizeof(u64) * kcap, 16);
+    L.off_tmp = take(sizeof(u64) * kcap, 16);
+    L.off_buf = take(sizeof(u64) * bcap, 16);
+    L.off_thresh = take(sizeof(u64), 8);
+    L.off_table = take(sizeof(float) * m * ks, 16);
+    L.off_xq = take(sizeof(float) * d, 16);
+    L.off_r = take(sizeof(float) * d, 16);
+    L.off_rn = take(sizeof(float) * m, 16);
+    L.off_prefix = take(sizeof(uint32_t) * (w + 1), 16);
+    L.off_plist = take(sizeof(int) * w, 16);
+    L.off_cand = take(sizeof(int) * kcap, 16);
+    L.off_cnt = take(sizeof(int) * 2, 8);
+    L.total = (o + 15) / 16 * 16;
+    return L;
+}
+
+// ADC sum of one code row: acc = 0; acc += T[s][code[s]] in s order
+template <int M>
+__device__ __forceinline__ float adc_row(const uint8_t* __restrict__ row, const float* __restrict__ T, int m,
+                                         int ks) {
+    float acc = 0.0f;
+    if constexpr (M == 4) {
+        uint32_t v = __ldg(reinterpret_cast<const uint32_t*>(row));
+#pragma unroll
+        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * ks + ((v >> (8 * s)) & 0xff)]);
+    } else if constexpr (M == 8) {
+        uint2 v = __ldg(reinterpret_cast<const uint2*>(row));
+#pragma unroll
+        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * ks + ((v.x >> (8 * s)) & 0xff)]);
+#pragma unroll
+        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[(s + 4) * ks + ((v.y >> (8 * s)) & 0xff)]);
+    } else if constexpr (M == 16) {
+        uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+#pragma unroll
+            for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[(4 * g + s) * ks + ((w4[g] >> (8 * s)) & 0xff)]);
+    } else {
+        for (int s = 0; s < m; s++) acc = __fadd_rn(acc, T[s * ks + row[s]]);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ int probe_of(const uint32_t* prefix, int w, uint32_t pos) {
+    // last j with prefix[j] <= pos
+    int lo = 0, hi = w;  // answer in [0, w-1]
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int M>
+__global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap, int bcap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* best = reinterpret_cast<u64*>(smem + L.off_best);
+    u64* tmp = reinterpret_cast<u64*>(smem + L.off_tmp);
+    u64* buf = reinterpret_cast<u64*>(smem + L.off_buf);
+    u64* thresh = reinterpret_cast<u64*>(smem + L.off_thresh);
+    float* table = reinterpret_cast<float*>(smem + L.off_table);
+    float* xq = reinterpret_cast<float*>(smem + L.off_xq);
+    float* r = reinterpret_cast<float*>(smem + L.off_r);
+    float* rn = reinterpret_cast<float*>(smem + L.off_rn);
+    uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.off_prefix);
+    int* plist = reinterpret_cast<int*>(smem + L.off_plist);
+    int* cand = reinterpret_cast<int*>(smem + L.off_cand);
+    int* cnt = reinterpret_cast<int*>(smem + L.off_cnt);
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap};
+
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const int d = ix.d, m = ix.m, ks = ix.ks, ds = ix.ds, w = a.w;
+    const bool src_res = a.flags & SCAN_SRC_RESIDUAL;
+    const bool direct = a.flags & SCAN_TABLE_DIRECT;
+    const bool rerank = a.flags & SCAN_RERANK;
+
+    if (!src_res)
+        for (int i = tid; i < d; i += SC_NT) xq[i] = a.queries[(int64_t)q * d + i];
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (int j = 0; j < w; j++) {
+            int l = a.probes[(int64_t)q * w + j];
+            plist[j] = l;
+            prefix[j] = acc;
+            acc += (l >= 0) ? (uint32_t)ix.list_len[l] : 0u;
+        }
+        prefix[w] = acc;
+    }
+    const int kk = rerank ? a.kl : a.k;
+    topk_init(s, kk);
+
+    for (int j = 0; j < w; j++) {
+        const int l = plist[j];
+        if (l < 0) continue;
+        // residual (bsxfunMINUS) or given residual row
+        if (src_res) {
+            const float* src = a.residual + ((int64_t)q * w + j) * d;
+            for (int i = tid; i < d; i += SC_NT) r[i] = src[i];
+        } else {
+            const float* cen = ix.coa + (int64_t)l * d;
+            for (int i = tid; i < d; i += SC_NT) r[i] = __fsub_rn(xq[i], cen[i]);
+        }
+        __syncthreads();
+        if (!direct)
+            for (int sq = tid; sq < m; sq += SC_NT) rn[sq] = norm_f_seq(r + sq * ds, ds);
+        __syncthreads();
+        // m x ks table (compute_cross_distances(ds, 1, ks, r_s, C_s))
+        for (int e = tid; e < m * ks; e += SC_NT) {
+            const int sq = e / ks;
+            const float* cen = ix.pq + (int64_t)e * ds;
+            const float* rs = r + sq * ds;
+            table[e] = direct ? direct_seq(rs, cen, ds) : expansion_from(ix.pq_norm[e], rn[sq], dot_seq(rs, cen, ds));
+        }
+        __syncthreads();
+        // ADC scan (sumidxtab2) with streaming top-k
+        const int len = ix.list_len[l];
+        const uint8_t* codes = ix.codes + ix.list_beg[l] * (int64_t)m;
+        const uint32_t pos0 = prefix[j];
+        for (int i0 = 0; i0 < len; i0 += SC_NT * SC_ITEMS) {
+#pragma unroll
+            for (int it = 0; it < SC_ITEMS; it++) {
+                const int i = i0 + it * SC_NT + tid;
+                const bool valid = i < len;
+                float dist = 0.0f;
+                if (valid) dist = adc_row<M>(codes + (int64_t)i * m, table, m, ks);
+                topk_offer(s, make_key(dist, pos0 + (uint32_t)i), valid);
+            }
+            topk_round_end(s, SC_NT * SC_ITEMS);
+        }
+        __syncthreads();
+    }
+    topk_finish(s);
+    const int nb = *s.nbest;
+
+    auto pos_to_id = [&](uint32_t pos) -> int32_t {
+        int j = probe_of(prefix, w, pos);
+        int l = plist[j];
+        return ix.ids[ix.list_beg[l] + (int64_t)(pos - prefix[j])];
+    };
+
+    if (!rerank) {
+        if (a.flags & SCAN_OUT_PACKED) {
+            const int64_t o = a.out_start[q];
+            for (int c = tid; c < nb; c += SC_NT) {
+                a.out_ids[o + c] = pos_to_id(key_payload(best[c]));
+                a.out_dis[o + c] = key_dist(best[c]);
+            }
+        } else {
+            for (int c = tid; c < a.k; c += SC_NT) {
+                a.out_ids[(int64_t)q * a.k + c] = c < nb ? pos_to_id(key_payload(best[c])) : -1;
+                a.out_dis[(int64_t)q * a.k + c] = c < nb ? key_dist(best[c]) : __int_as_float(0x7f800000);
+            }
+        }
+        return;
+    }
+
+    // RERANK (ivf_search.cpp:113-134): exact L2 of the ktmp = nb candidates
+    for (int c = tid; c < nb; c += SC_NT) cand[c] = pos_to_id(key_payload(best[c]));
+    __syncthreads();
+    const int kr = min(a.k, nb);
+    if (kr > 0) {
+        topk_init(s, kr);
+        const double qn = a.qnorm[q];
+        for (int c0 = 0; c0 < nb; c0 += SC_NT) {
+            const int c = c0 + tid;
+            const bool valid = c < nb;
+            float dist = 0.0f;
+            if (valid) {
+                const int32_t id = cand[c];
+                const float* v = ix.base + (int64_t)id * d;
+                dist = expansion_from(qn, ix.base_norm[id], dot_seq(v, xq, d));
+            }
+            topk_offer(s, make_key(dist, (uint32_t)c), valid);
+            topk_round_end(s, SC_NT);
+        }
+        topk_finish(s);
+    }
+    for (int c = tid; c < a.k; c += SC_NT) {
+        a.out_ids[(int64_t)q * a.k + c] = c < kr ? cand[key_payload(best[c])] : -1;
+        a.out_dis[(int64_t)q * a.k + c] = c < kr ? key_dist(best[c]) : __int_as_float(0x7f800000);
+    }
+}
+
+template <int M>
+static cudaError_t launch_scan_m(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
+    const bool rerank = a.flags & SCAN_RERANK;
+    const int kk = rerank ? a.kl : a.k;
+    int kcap = pow2_at_least(std::max(std::max(kk, a.k), 2));
+    int bcap = pow2_at_least(std::max(2048, kcap));
+    ScanSmem L = scan_smem_layout(ix.m, ix.ks, ix.d, a.w, kcap, bcap);
+    auto kern = ivf_scan_kernel<M>;
+    if (L.total > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<a.nq, SC_NT, L.total, st>>>(ix, a, L, kcap, bcap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
+    if (a.nq <= 0) return cudaSuccess;
+    switch (ix.m) {
+        case 4: return launch_scan_m<4>(ix, a, st);
+        case 8: return launch_scan_m<8>(ix, a, st);
+        case 16: return launch_scan_m<16>(ix, a, st);
+        default: return launch_scan_m<0>(ix, a, st);
+    }
+}
+
+}  // namespace gbivf

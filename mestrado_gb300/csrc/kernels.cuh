@@ -1,0 +1,61 @@
+// Kernel launch interface of the GB300 IVF-PQ engine (internal; the public
+// surface is the C ABI in include/gbivf.h).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbivf {
+
+enum ScanFlags : int {
+    SCAN_RERANK = 1,        // exact L2 re-rank of the kl ADC candidates
+    SCAN_TABLE_DIRECT = 2,  // tables as sum (r-c)^2 (parallel2 core)
+    SCAN_SRC_RESIDUAL = 4,  // residuals are given (nq*w x d) instead of queries
+    SCAN_OUT_PACKED = 8,    // write min(L, k) results at out_start[q] (core_gpu)
+};
+
+// Device view of one index (all pointers in device memory).
+struct DevIndex {
+    int d = 0, C = 0, m = 0, ks = 0, ds = 0;
+    int64_t rows = 0;             // code rows incl. alignment padding
+    const float* coa = nullptr;        // C x d
+    const float* coa_norm = nullptr;   // C   float norms (a-operand of the coarse product)
+    const float* pq = nullptr;         // m x ks x ds
+    const double* pq_norm = nullptr;   // m x ks double norms (b-operand of the table product)
+    const int64_t* list_beg = nullptr; // C   first row of each list
+    const int32_t* list_len = nullptr; // C
+    const uint8_t* codes = nullptr;    // rows x m
+    const int32_t* ids = nullptr;      // rows (-1 in padding)
+    const float* base = nullptr;       // nbase x d raw vectors (re-rank)
+    const float* base_norm = nullptr;  // nbase float norms
+    int64_t nbase = 0;
+};
+
+struct ScanArgs {
+    int nq = 0, w = 0, k = 0, kl = 0, flags = 0;
+    const float* queries = nullptr;    // nq x d
+    const double* qnorm = nullptr;     // nq
+    const int32_t* probes = nullptr;   // nq x w list ids (coaidx / rid_to_ivf)
+    const float* residual = nullptr;   // (nq*w) x d when SCAN_SRC_RESIDUAL
+    const int32_t* out_start = nullptr;// nq when SCAN_OUT_PACKED
+    int32_t* out_ids = nullptr;
+    float* out_dis = nullptr;
+};
+
+// query norms: double accumulation of float squares (nn.c:137-142)
+cudaError_t launch_norm_d(const float* x, int64_t n, int d, double* out, cudaStream_t st);
+// row norms: float, sequential (nn.c:129-135)
+cudaError_t launch_norm_f(const float* x, int64_t n, int d, float* out, cudaStream_t st);
+// coarse distances of nq queries to all C centroids: out nq x C
+cudaError_t launch_coarse_dist(const DevIndex& ix, const float* q, const double* qnorm, int nq,
+                               float* out, cudaStream_t st);
+// per query, the w smallest (distance, centroid) of a nq x C distance block
+cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_t* coaidx,
+                                 float* coadis, cudaStream_t st);
+// fused residual + table + ADC scan + top-k (+ re-rank), one CTA per query
+cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
+
+// largest k / kl / w the scan kernel supports
+constexpr int MAX_K = 2048;
+constexpr int MAX_W = 4096;
+
+}  // namespace gbivf

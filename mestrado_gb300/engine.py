@@ -1,0 +1,155 @@
+"""Python mirror of the reference's IVF-PQ search entry points, on the GPU.
+
+Each function keeps the reference's name, argument meaning and output
+convention, and runs through the C ABI (include/gbivf.h):
+
+* :func:`ivfpq_search` -- ``ivfpq_search(ivfpq, ivf, vquery, vbase, k, kl, w,
+  ids, dis)`` (sequential/ivf_pq/ivf_search.cpp:9);
+* :func:`pq_search` -- ``pq_search(pq, codebook, vquery, k, dis, ids)``
+  (sequential/pq-utils/pq_search.cpp:10);
+* :func:`core_gpu` -- ``core_gpu(PQ, residual, ivf, ivf_size, rid_to_ivf,
+  qid_to_starting_outid, idxs, dists, k, w)`` (parallel2/ivf_pq/mycuda.cu:119).
+
+Errors raise :class:`GbivfError` (the reference exits the process instead).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import GBIVF_RERANK, GBIVF_TABLE_DIRECT, GbivfError, check  # noqa: F401
+from .ivfdata import IVFPQData
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+class GpuIndex:
+    """An IVF-PQ index resident in GPU memory (the handle owns it)."""
+
+    def __init__(self, data: IVFPQData, device: int = 0, base: np.ndarray | None = None):
+        data.validate()
+        self.lib = _lib.load()
+        self.data = data
+        self.device = device
+        h = C.c_void_p()
+        keep = [_c(data.coa, np.float32), _c(data.pq, np.float32), _c(data.list_off, np.int64),
+                _c(data.ids, np.int32), _c(data.codes, np.uint8)]
+        check(self.lib.gbivf_index_create(C.byref(h), device, data.d, data.coarsek, _p(keep[0]), data.m,
+                                          data.ks, _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4])))
+        self.h = h
+        self.base_rows = 0
+        if base is not None:
+            self.set_base(base)
+
+    @classmethod
+    def from_handle(cls, h: C.c_void_p, device: int = 0) -> "GpuIndex":
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.data = None
+        self.device = device
+        self.h = h
+        return self
+
+    def set_base(self, base: np.ndarray) -> None:
+        b = _c(base, np.float32)
+        check(self.lib.gbivf_index_set_base(self.h, _p(b), b.shape[0], b.shape[1]))
+        self.base_rows = b.shape[0]
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gbivf_index_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def dims(self):
+        d, c, m, ks = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        n = C.c_int64()
+        check(self.lib.gbivf_index_dims(self.h, C.byref(d), C.byref(c), C.byref(m), C.byref(ks), C.byref(n)))
+        return d.value, c.value, m.value, ks.value, n.value
+
+    # -- searches ---------------------------------------------------------
+    def search(self, queries, k, w, kl=None, rerank=False, direct=False):
+        """ivfpq_search: (ids nq x k int32, dis nq x k float32)."""
+        q = _c(queries, np.float32)
+        nq = q.shape[0]
+        ids = np.empty((nq, k), np.int32)
+        dis = np.empty((nq, k), np.float32)
+        flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
+        check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
+                                          _p(ids), _p(dis)))
+        return ids, dis
+
+    def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
+                      stream_ptr=0):
+        """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
+        flags = GBIVF_RERANK if rerank else 0
+        check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
+                                                 kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
+                                                 C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
+
+    def coarse_assign(self, queries, w):
+        q = _c(queries, np.float32)
+        nq = q.shape[0]
+        idx = np.empty((nq, w), np.int32)
+        dis = np.empty((nq, w), np.float32)
+        check(self.lib.gbivf_coarse_assign(self.h, _p(q), nq, w, _p(idx), _p(dis)))
+        return idx, dis
+
+    def core_gpu(self, residual, rid_to_ivf, qid_to_starting_outid, nout, k, w):
+        r = _c(residual, np.float32)
+        rid = _c(rid_to_ivf, np.int32)
+        qs = _c(qid_to_starting_outid, np.int32)
+        idxs = np.full(nout, -1, np.int32)
+        dists = np.full(nout, np.nan, np.float32)
+        check(self.lib.gbivf_core_gpu(self.h, _p(r), r.shape[0], _p(rid), _p(qs), _p(idxs), _p(dists), k, w))
+        return idxs, dists
+
+
+class GpuPQ(GpuIndex):
+    """A flat PQ codebook resident in GPU memory (pq_search)."""
+
+    def __init__(self, pq: np.ndarray, codes: np.ndarray, device: int = 0):
+        self.lib = _lib.load()
+        self.data = None
+        self.device = device
+        pqc = _c(pq, np.float32)
+        cb = _c(codes, np.uint8)
+        m, ks, ds = pqc.shape
+        h = C.c_void_p()
+        check(self.lib.gbivf_pq_create(C.byref(h), device, m * ds, m, ks, _p(pqc), _p(cb), cb.shape[0]))
+        self.h = h
+        self.d = m * ds
+
+    def pq_search(self, queries, k):
+        q = _c(queries, np.float32)
+        nq = q.shape[0]
+        dis = np.empty((k, nq), np.float32)
+        ids = np.empty((k, nq), np.int32)
+        check(self.lib.gbivf_pq_search(self.h, _p(q), nq, k, _p(dis), _p(ids)))
+        return dis, ids
+
+
+def ivfpq_search(index: GpuIndex, vquery, vbase, k, kl, w):
+    """The reference signature's semantics: always re-ranks kl -> k against
+    vbase (uploaded once per index). Returns (ids, dis)."""
+    if getattr(index, "base_rows", 0) != len(vbase):
+        index.set_base(vbase)
+    return index.search(vquery, k, w, kl=kl, rerank=True)
+
+
+def pq_search(pq, codebook, vquery, k):
+    """pq_search with the reference's outputs: (dis, ids), k x nq, ids 1-based."""
+    return GpuPQ(pq, codebook).pq_search(vquery, k)
