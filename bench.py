@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the IVF-PQ search path (ivfpq_search drop-in) on GB300.
+
+Workload (default ``--config cfg2``): plain FP32 ivfpq_search over a 1M-vector
+index -- base 1,000,000 x d=128 from a 1,024-component Gaussian mixture
+(means U[0,120], sigma 20, clipped to [0,255], rounded; seed 0), 100,000
+training vectors, C = 1,024 lists, m = 8 x 256 codes, 10,000 queries per
+step, w = 16 probes, k = 100, re-rank of kl = 100 ADC candidates.
+The synthetic mixture stands in for the reference's SIFT runs.
+
+A step is one search of the whole 10,000-query batch.
+
+* ``value``: QPS with queries, index and outputs resident in HBM, CUDA
+  events around each step on the launching stream, L2 flushed (a 256 MB
+  write) between steps outside the timed events.
+* ``e2e``: QPS through the host C ABI call (gbivf_ivfpq_search): queries
+  copied from pinned host memory, ids and distances copied back, per step.
+* ``roofline``: the fused scan kernel (ivf_scan_kernel) -- algorithmic bytes
+  = sum over queries of the probed lists' code bytes (n_l * m) divided by
+  the kernel's CUDA-event time, against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the CPU oracle (plain-C restatement of the reference's
+  ivfpq_search) on the host cores, OpenMP over queries.
+
+``--impl reference`` times that CPU implementation alone, in steps of a
+bounded sample of the same queries.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+CONFIGS = {
+    "cfg2": dict(d=128, ncomp=1024, seed=0, nbase=1_000_000, ntrain=100_000, nq=10_000, C=1024, m=8,
+                 w=16, k=100, kl=100, rerank=True, train_iters=10),
+    "cfg1": dict(d=128, ncomp=64, seed=0, nbase=10_000, ntrain=5_000, nq=100, C=16, m=8,
+                 w=4, k=100, kl=100, rerank=True, train_iters=10),
+}
+
+CACHE = os.environ.get("MESTRADO_GB300_CACHE", "/tmp/mestrado_gb300_cache")
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_name(c):
+    return (f"ivfpq_search plain fp32: base {c['nbase']:,} x d={c['d']} ({c['ncomp']}-component mixture), "
+            f"C={c['C']} lists, m={c['m']}x256, {c['nq']:,} queries/step, w={c['w']}, k={c['k']}, "
+            f"rerank kl={c['kl']}")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+
+def make_inputs(c, rank=0):
+    """(index data, base, queries): cached on local disk by config."""
+    from mestrado_gb300.ivfdata import IVFPQData
+    from mestrado_gb300.synth import STREAM_QUERY, Mixture
+    from mestrado_gb300.train import build_index
+
+    key = hashlib.sha1(json.dumps({k: c[k] for k in sorted(c)}, sort_keys=True).encode()).hexdigest()[:12]
+    os.makedirs(CACHE, exist_ok=True)
+    ipath = os.path.join(CACHE, f"index_{key}.npz")
+    mx = Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"])
+    means = mx.means()
+    base = mx.base(c["nbase"], means)
+    # each rank searches its own query batch (weak scaling)
+    queries = mx.sample(STREAM_QUERY, c["nq"], chunk=rank, means=means)
+    if os.path.exists(ipath):
+        ix = IVFPQData.load(ipath)
+    else:
+        t = time.time()
+        train = mx.train(c["ntrain"], means)
+        ix = build_index(train, base, c["C"], c["m"], niter=c["train_iters"], seed=c["seed"])
+        tmp = ipath + f".{os.getpid()}.npz"
+        ix.save(tmp)
+        os.replace(tmp, ipath)
+        log(f"index built in {time.time() - t:.1f}s")
+    return ix, base, queries, key
+
+
+def ground_truth(base, queries, k, key, device):
+    """Exact FP64 brute-force top-k on the GPU (evaluation only)."""
+    import torch
+
+    path = os.path.join(CACHE, f"gt_{key}_{hashlib.sha1(queries.tobytes()).hexdigest()[:8]}_{k}.npy")
+    if os.path.exists(path):
+        return np.load(path)
+    b = torch.from_numpy(base).to(device, torch.float64)
+    bn = (b * b).sum(1)
+    out = np.empty((len(queries), k), np.int64)
+    for s in range(0, len(queries), 1024):
+        q = torch.from_numpy(queries[s:s + 1024]).to(device, torch.float64)
+        dist = (q * q).sum(1, keepdim=True) + bn[None, :] - 2.0 * (q @ b.T)
+        out[s:s + len(q)] = torch.topk(dist, k, dim=1, largest=False).indices.cpu().numpy()
+    del b
+    np.save(path, out)
+    return out
+
+
+def recall_report(ids, gt, k):
+    hits = np.array([len(set(a[a >= 0].tolist()) & set(b[:k].tolist())) for a, b in zip(ids, gt)])
+    # R@r as the reference prints it: share of queries whose true 1-NN is in the top r
+    # (sequential/pq-utils/pq_test_compute_stats.cpp:76-149)
+    r_at = {f"R@{r}": float(np.mean([(gt[i, 0] in ids[i, :r]) for i in range(len(ids))])) for r in (1, 10, 100)
+            if r <= ids.shape[1]}
+    return {f"recall@{k}": float(hits.mean() / k), **r_at}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(config_name):
+    """DRAM bytes per scan-kernel launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"ivf_scan_{config_name}.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch"):
+                return float(line.split("=")[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restatement of the reference, all host threads)
+# ---------------------------------------------------------------------------
+
+def cpu_search(ix, base, queries, c, nthreads):
+    import oracle
+
+    t = time.perf_counter()
+    oracle.ivfpq_search(ix, queries, k=c["k"], kl=c["kl"], w=c["w"], base=base, rerank=c["rerank"],
+                        nthreads=nthreads)
+    return time.perf_counter() - t
+
+
+def run_reference(args, c, rank, world):
+    if rank != 0:
+        return
+    ix, base, queries, _ = make_inputs(c, 0)
+    nthreads = os.cpu_count() or 1
+    sample = min(len(queries), args.ref_sample)
+    qs = queries[:sample]
+    for _ in range(args.warmup):
+        cpu_search(ix, base, qs[: max(1, sample // 10)], c, nthreads)
+    ts = [cpu_search(ix, base, qs, c, nthreads) for _ in range(args.steps)]
+    total = sum(ts)
+    qps = sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": "QPS", "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": workload_name(c), "sample_queries_per_step": sample},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{sample} of the {c['nq']} queries per step"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU engine
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, c, rank, world, local_rank):
+    import torch
+
+    from mestrado_gb300.engine import GpuIndex
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    ix_data, base, queries, key = make_inputs(c, rank)
+    nq, k, kl, w, m = c["nq"], c["k"], c["kl"], c["w"], c["m"]
+
+    # CPU baseline first (rank 0, N=1), before any GPU work in this process
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        sample = min(nq, args.ref_sample)
+        cpu_search(ix_data, base, queries[: max(1, sample // 10)], c, nthreads)
+        t = cpu_search(ix_data, base, queries[:sample], c, nthreads)
+        cpu = {"value": sample / t, "unit": "queries/s", "cores": nthreads, "kind": "port",
+               "sample": f"{sample} queries of this workload, OpenMP over queries ({t:.2f}s)"}
+
+    gi = GpuIndex(ix_data, device=local_rank, base=base)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    d_q = torch.from_numpy(queries).to(dev)
+    d_ids = torch.empty((nq, k), dtype=torch.int32, device=dev)
+    d_dis = torch.empty((nq, k), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step(profile):
+        gi.search_device(d_q.data_ptr(), nq, k, w, d_ids.data_ptr(), d_dis.data_ptr(), kl=kl,
+                         rerank=c["rerank"], stream_ptr=sp, profile=profile)
+
+    # algorithmic scan bytes: sum over queries of the probed lists' codes
+    coaidx, _ = gi.coarse_assign(queries, w)
+    sizes = ix_data.list_sizes().astype(np.int64)
+    scan_bytes = int(sizes[coaidx].sum()) * m
+
+    for i in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xff)
+        step(True)
+    stream.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    barrier()
+    step_ms, scan_ms, coarse_ms = [], [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_((i + 1) & 0xff)  # L2 flush, outside the timed events
+            ev0.record(stream)
+        step(True)
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        cm, sm = gi.last_stage_ms()
+        coarse_ms.append(cm)
+        scan_ms.append(sm)
+    barrier()
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = nq * args.steps * world / (total_ms / 1000.0)
+
+    # end to end through the host C ABI: pinned host queries in, ids/dis out
+    h_q = torch.from_numpy(queries).pin_memory().numpy()
+    h_ids = torch.empty((nq, k), dtype=torch.int32).pin_memory().numpy()
+    h_dis = torch.empty((nq, k), dtype=torch.float32).pin_memory().numpy()
+    for _ in range(2):
+        gi.search(h_q, k, w, kl=kl, rerank=c["rerank"], out=(h_ids, h_dis))
+    e2e_s = 0.0
+    for i in range(args.steps):
+        flush.fill_((i + 7) & 0xff)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        gi.search(h_q, k, w, kl=kl, rerank=c["rerank"], out=(h_ids, h_dis))
+        e2e_s += time.perf_counter() - t
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = nq * args.steps * world / e2e_s
+
+    # quality (outside every timed region)
+    quality = {}
+    if rank == 0 and not args.no_recall:
+        gt = ground_truth(base, queries, k, key, dev)
+        quality = recall_report(h_ids, gt, k)
+
+    peak, peak_kind = measured_peak_hbm()
+    mean_scan_s = statistics.mean(scan_ms) / 1000.0
+    achieved = scan_bytes / mean_scan_s / 1e9
+    traffic = profiled_traffic(args.config)
+    if rank == 0:
+        line = {
+            "metric": "QPS", "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(c), "queries_per_step": nq, "parallelism": f"replica x{world}",
+                       "l2": "flushed between steps (256 MB write)", **quality,
+                       "stage_ms": {"coarse": statistics.mean(coarse_ms), "scan": statistics.mean(scan_ms)}},
+            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(queries.nbytes),
+                    "d2h_bytes_per_step": int(nq * k * 8)},
+            "roofline": {"bound": "hbm", "kernel": "ivf_scan_kernel", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "bytes_per_launch": scan_bytes, "traffic": traffic},
+            "cpu_baseline": cpu,
+            "gpu_launches": 4 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    gi.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbivf", choices=["gbivf", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
+    ap.add_argument("--ref-sample", type=int, default=10_000, help="queries per CPU step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-recall", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log(f"--warmup {args.warmup} raised to 3 (at least 3 untimed warm-up steps)")
+        args.warmup = 3
+    c = CONFIGS[args.config]
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, c, rank, world)
+    else:
+        run_gpu(args, c, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -40,6 +40,7 @@ extern "C" {
 /* search flags */
 #define GBIVF_RERANK 0x1u       /* exact L2 re-rank of the kl ADC candidates to k */
 #define GBIVF_TABLE_DIRECT 0x2u /* tables as sum (r-c)^2 (parallel2) instead of the expansion */
+#define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 
 typedef struct gbivf_index gbivf_index;
 
@@ -95,6 +96,13 @@ int gbivf_ivfpq_search(gbivf_index *ix, const float *queries, int nq, int k, int
  * the default stream); returns after launching. */
 int gbivf_ivfpq_search_device(gbivf_index *ix, const float *d_queries, int nq, int k, int kl,
                               int w, unsigned flags, int32_t *d_ids, float *d_dis, void *stream);
+
+/* Stage times (milliseconds, CUDA events on the launching stream) of the
+ * last search made with GBIVF_PROFILE: coarse assignment (query norms,
+ * distances, k-min) and the fused scan (tables, ADC, top-k, re-rank).
+ * Waits for that search to finish. No counterpart in the reference, which
+ * prints gettimeofday deltas (sequential/ivf_pq/ivf_search.cpp:105-111). */
+int gbivf_last_stage_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms);
 
 /* The coarse stage alone: knn_full(2, nq, C, d, w, coa, queries, ...)
  * (sequential/ivf_pq/ivf_search.cpp:37-38): the w nearest lists per query,

@@ -13,6 +13,7 @@ from . import build as _build
 GBIVF_OK = 0
 GBIVF_RERANK = 0x1
 GBIVF_TABLE_DIRECT = 0x2
+GBIVF_PROFILE = 0x100
 
 _lib = None
 
@@ -21,7 +22,7 @@ EXPORTS = [
     "gbivf_last_error", "gbivf_version", "gbivf_index_create", "gbivf_index_create_from_lists",
     "gbivf_index_set_base", "gbivf_index_destroy", "gbivf_index_dims", "gbivf_ivfpq_search",
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
-    "gbivf_pq_search",
+    "gbivf_pq_search", "gbivf_last_stage_ms",
 ]
 
 
@@ -56,6 +57,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_core_gpu.argtypes = [vp, vp, i32, vp, vp, vp, vp, i32, i32]
     lib.gbivf_pq_create.argtypes = [C.POINTER(vp), i32, i32, i32, i32, vp, vp, i64]
     lib.gbivf_pq_search.argtypes = [vp, vp, i32, i32, vp, vp]
+    lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     for name in EXPORTS:
         if name != "gbivf_last_error":
             getattr(lib, name).restype = i32

@@ -22,7 +22,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libgbivf.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["kernels.cu", "api.cu"]
+SOURCES = ["kernels.cu", "scan_persistent.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",

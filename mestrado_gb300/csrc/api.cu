@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/gbivf.h"
+#include "exact_round.cuh"
 #include "kernels.cuh"
 
 using namespace gbivf;
@@ -105,14 +106,16 @@ struct gbivf_index {
     DevIndex dx;
     std::vector<int32_t> h_len;  // list sizes (host copy)
     int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
+    int num_sms = 0;
+    bool use_persistent = true;       // register-codebook scan where the shape allows
     std::vector<void*> owned;    // index allocations
     DBuf base, base_norm;
     cudaStream_t stream = nullptr;
     std::mutex mu;
     // workspace
-    DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start;
-    std::vector<int32_t> h_tmp_ids;
-    std::vector<float> h_tmp_dis;
+    DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
+    bool ev_valid = false;
 };
 
 namespace {
@@ -132,10 +135,12 @@ void free_index(gbivf_index* ix) {
     for (void* p : ix->owned) cudaFree(p);
     ix->owned.clear();
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
-                    &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start})
+                    &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
+    for (auto& e : ix->ev)
+        if (e) cudaEventDestroy(e), e = nullptr;
 }
 
 int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
@@ -195,7 +200,12 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     std::vector<float> cn(coarsek);
     for (int c = 0; c < coarsek; c++) cn[c] = norm_f_host(coa + (int64_t)c * d, d);
     std::vector<double> pn((size_t)nsq * ks);
-    for (int e = 0; e < nsq * ks; e++) pn[e] = norm_d_host(pq + (int64_t)e * ds, ds);
+    std::vector<float> phi((size_t)nsq * ks), plo((size_t)nsq * ks);
+    for (int e = 0; e < nsq * ks; e++) {
+        pn[e] = norm_d_host(pq + (int64_t)e * ds, ds);
+        split_norm(pn[e], &phi[e], &plo[e]);
+    }
+    if (cudaDeviceGetAttribute(&ix->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) ix->num_sms = 1;
 
     DevIndex& dx = ix->dx;
     dx.d = d;
@@ -205,7 +215,7 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     dx.ds = ds;
     dx.rows = rows;
     cudaError_t e = cudaSuccess;
-    float *p_coa, *p_cn, *p_pq;
+    float *p_coa, *p_cn, *p_pq, *p_phi, *p_plo;
     double* p_pn;
     int64_t* p_beg;
     int32_t *p_len, *p_ids;
@@ -214,6 +224,8 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         (e = upload(ix, cn.data(), cn.size(), &p_cn)) != cudaSuccess ||
         (e = upload(ix, pq, (size_t)nsq * ks * ds, &p_pq)) != cudaSuccess ||
         (e = upload(ix, pn.data(), pn.size(), &p_pn)) != cudaSuccess ||
+        (e = upload(ix, phi.data(), phi.size(), &p_phi)) != cudaSuccess ||
+        (e = upload(ix, plo.data(), plo.size(), &p_plo)) != cudaSuccess ||
         (e = upload(ix, beg.data(), beg.size(), &p_beg)) != cudaSuccess ||
         (e = upload(ix, ix->h_len.data(), ix->h_len.size(), &p_len)) != cudaSuccess ||
         (e = upload(ix, pcodes.data(), pcodes.size(), &p_codes)) != cudaSuccess ||
@@ -227,6 +239,8 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     dx.coa_norm = p_cn;
     dx.pq = p_pq;
     dx.pq_norm = p_pn;
+    dx.pq_hi = p_phi;
+    dx.pq_lo = p_plo;
     dx.list_beg = p_beg;
     dx.list_len = p_len;
     dx.codes = p_codes;
@@ -243,13 +257,25 @@ int coarse_batch(int nq, int C) {
     return (int)std::max<int64_t>(1, bq);
 }
 
+// the persistent register-codebook kernel where it applies, else the general one
+int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
+    CK(ix->w_queue.ensure(sizeof(int)));
+    a.queue = ix->w_queue.as<int>();
+    if (ix->use_persistent && scan_persistent_supported(ix->dx, a)) {
+        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, st));
+    } else {
+        CK(launch_scan(ix->dx, a, st));
+    }
+    return GBIVF_OK;
+}
+
 int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) {
     if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
     if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
     if (k <= 0 || k > MAX_K) return fail(k <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "k=%d (1..%d)", k, MAX_K);
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
-    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
     if (flags & GBIVF_RERANK) {
         if (kl <= 0 || kl > MAX_K) return fail(kl <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "kl=%d (1..%d)", kl, MAX_K);
         if (!ix->base.p) return fail(GBIVF_ERR_INVALID, "GBIVF_RERANK needs gbivf_index_set_base first");
@@ -271,6 +297,13 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     double* qn = ix->w_qn.as<double>();
     int32_t* coaidx = ix->w_coaidx.as<int32_t>();
     float* coadis = ix->w_coadis.as<float>();
+    const bool prof = flags & GBIVF_PROFILE;
+    if (prof) {
+        for (auto& e : ix->ev)
+            if (!e) CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(ix->ev[0], st));
+    }
+    ix->ev_valid = false;
     CK(launch_norm_d(d_q, nq, dx.d, qn, st));
     if (dx.C == 1) {
         CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
@@ -295,7 +328,15 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.probes = coaidx;
     a.out_ids = d_ids;
     a.out_dis = d_dis;
-    CK(launch_scan(dx, a, st));
+    if (prof) CK(cudaEventRecord(ix->ev[1], st));
+    {
+        int rs = run_scan(ix, a, st);
+        if (rs) return rs;
+    }
+    if (prof) {
+        CK(cudaEventRecord(ix->ev[2], st));
+        ix->ev_valid = true;
+    }
     return GBIVF_OK;
 }
 
@@ -418,6 +459,19 @@ int gbivf_ivfpq_search(gbivf_index* ix, const float* queries, int nq, int k, int
     return GBIVF_OK;
 }
 
+int gbivf_last_stage_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (!ix->ev_valid) return fail(GBIVF_ERR_INVALID, "no search with GBIVF_PROFILE since the last one without");
+    DeviceGuard g(ix->device);
+    CK(cudaEventSynchronize(ix->ev[2]));
+    float a = 0, b = 0;
+    CK(cudaEventElapsedTime(&a, ix->ev[0], ix->ev[1]));
+    CK(cudaEventElapsedTime(&b, ix->ev[1], ix->ev[2]));
+    if (coarse_ms) *coarse_ms = a;
+    if (scan_ms) *scan_ms = b;
+    return GBIVF_OK;
+}
+
 int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, int32_t* coaidx, float* coadis) {
     if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
     if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
@@ -491,7 +545,8 @@ int gbivf_core_gpu(gbivf_index* ix, const float* residual, int nres, const int32
     a.out_start = ix->w_start.as<int32_t>();
     a.out_ids = ix->w_ids.as<int32_t>();
     a.out_dis = ix->w_dis.as<float>();
-    CK(launch_scan(dx, a, ix->stream));
+    int rc = run_scan(ix, a, ix->stream);
+    if (rc) return rc;
     // copy back only the written ranges
     for (int q = 0; q < nq; q++) {
         int64_t L = 0;

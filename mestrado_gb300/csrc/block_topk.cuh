@@ -66,7 +66,7 @@ __device__ __forceinline__ int lower_bound_u64(const u64* a, int n, u64 x) {
     return lo;
 }
 
-__device__ void bitonic_sort_smem(u64* a, int n) {
+__device__ inline void bitonic_sort_smem(u64* a, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int size = 2; size <= n; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -86,7 +86,7 @@ __device__ void bitonic_sort_smem(u64* a, int n) {
 }
 
 // Merge the nb buffered keys into best. nb is the block-uniform count.
-__device__ void topk_flush(TopKSmem& s, int nb) {
+__device__ inline void topk_flush(TopKSmem& s, int nb) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if (nb <= 0) return;
     int n = 2;

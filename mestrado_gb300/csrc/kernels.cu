@@ -12,8 +12,7 @@
 // broken by (distance, payload) keys (block_topk.cuh).
 #include <algorithm>
 
-#include "block_topk.cuh"
-#include "kernels.cuh"
+#include "scan_common.cuh"
 
 namespace gbivf {
 
@@ -119,12 +118,6 @@ cudaError_t launch_coarse_dist(const DevIndex& ix, const float* q, const double*
 
 constexpr int CS_NT = 128, CS_ITEMS = 8;
 
-static int pow2_at_least(int x) {
-    int n = 1;
-    while (n < x) n <<= 1;
-    return n;
-}
-
 __global__ void __launch_bounds__(CS_NT) coarse_select_kernel(
     const float* __restrict__ dist, int C, int w, int kcap, int bcap,
     int32_t* __restrict__ coaidx, float* __restrict__ coadis) {
@@ -173,79 +166,10 @@ cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_
 // ---------------------------------------------------------------------------
 // fused scan: per query (one CTA), for each probed list: residual, m x ks
 // table in shared memory, ADC over the list's codes, streaming top-k; then
-// the optional exact re-rank of the kl best.
+// the optional exact re-rank of the kl best. General shapes (any d, m, ks).
 // ---------------------------------------------------------------------------
 
 constexpr int SC_NT = 256, SC_ITEMS = 4;
-
-struct ScanSmem {
-    size_t off_best, off_tmp, off_buf, off_thresh, off_table, off_xq, off_r, off_rn, off_prefix,
-        off_plist, off_cand, off_cnt, total;
-};
-
-static ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap) {
-    ScanSmem L;
-    size_t o = 0;
-    auto take = [&](size_t bytes, size_t align) {
-        o = (o + align - 1) / align * align;
-        size_t r = o;
-        o += bytes;
-        return r;
-    };
-    L.off_best = take(sizeof(u64) * kcap, 16);
-    L.off_tmp = take(sizeof(u64) * kcap, 16);
-    L.off_buf = take(sizeof(u64) * bcap, 16);
-    L.off_thresh = take(sizeof(u64), 8);
-    L.off_table = take(sizeof(float) * m * ks, 16);
-    L.off_xq = take(sizeof(float) * d, 16);
-    L.off_r = take(sizeof(float) * d, 16);
-    L.off_rn = take(sizeof(float) * m, 16);
-    L.off_prefix = take(sizeof(uint32_t) * (w + 1), 16);
-    L.off_plist = take(sizeof(int) * w, 16);
-    L.off_cand = take(sizeof(int) * kcap, 16);
-    L.off_cnt = take(sizeof(int) * 2, 8);
-    L.total = (o + 15) / 16 * 16;
-    return L;
-}
-
-// ADC sum of one code row: acc = 0; acc += T[s][code[s]] in s order
-template <int M>
-__device__ __forceinline__ float adc_row(const uint8_t* __restrict__ row, const float* __restrict__ T, int m,
-                                         int ks) {
-    float acc = 0.0f;
-    if constexpr (M == 4) {
-        uint32_t v = __ldg(reinterpret_cast<const uint32_t*>(row));
-#pragma unroll
-        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * ks + ((v >> (8 * s)) & 0xff)]);
-    } else if constexpr (M == 8) {
-        uint2 v = __ldg(reinterpret_cast<const uint2*>(row));
-#pragma unroll
-        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * ks + ((v.x >> (8 * s)) & 0xff)]);
-#pragma unroll
-        for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[(s + 4) * ks + ((v.y >> (8 * s)) & 0xff)]);
-    } else if constexpr (M == 16) {
-        uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
-        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int g = 0; g < 4; g++)
-#pragma unroll
-            for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[(4 * g + s) * ks + ((w4[g] >> (8 * s)) & 0xff)]);
-    } else {
-        for (int s = 0; s < m; s++) acc = __fadd_rn(acc, T[s * ks + row[s]]);
-    }
-    return acc;
-}
-
-__device__ __forceinline__ int probe_of(const uint32_t* prefix, int w, uint32_t pos) {
-    // last j with prefix[j] <= pos
-    int lo = 0, hi = w;  // answer in [0, w-1]
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= pos) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 
 template <int M>
 __global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap, int bcap) {
@@ -326,55 +250,7 @@ __global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a
         __syncthreads();
     }
     topk_finish(s);
-    const int nb = *s.nbest;
-
-    auto pos_to_id = [&](uint32_t pos) -> int32_t {
-        int j = probe_of(prefix, w, pos);
-        int l = plist[j];
-        return ix.ids[ix.list_beg[l] + (int64_t)(pos - prefix[j])];
-    };
-
-    if (!rerank) {
-        if (a.flags & SCAN_OUT_PACKED) {
-            const int64_t o = a.out_start[q];
-            for (int c = tid; c < nb; c += SC_NT) {
-                a.out_ids[o + c] = pos_to_id(key_payload(best[c]));
-                a.out_dis[o + c] = key_dist(best[c]);
-            }
-        } else {
-            for (int c = tid; c < a.k; c += SC_NT) {
-                a.out_ids[(int64_t)q * a.k + c] = c < nb ? pos_to_id(key_payload(best[c])) : -1;
-                a.out_dis[(int64_t)q * a.k + c] = c < nb ? key_dist(best[c]) : __int_as_float(0x7f800000);
-            }
-        }
-        return;
-    }
-
-    // RERANK (ivf_search.cpp:113-134): exact L2 of the ktmp = nb candidates
-    for (int c = tid; c < nb; c += SC_NT) cand[c] = pos_to_id(key_payload(best[c]));
-    __syncthreads();
-    const int kr = min(a.k, nb);
-    if (kr > 0) {
-        topk_init(s, kr);
-        const double qn = a.qnorm[q];
-        for (int c0 = 0; c0 < nb; c0 += SC_NT) {
-            const int c = c0 + tid;
-            const bool valid = c < nb;
-            float dist = 0.0f;
-            if (valid) {
-                const int32_t id = cand[c];
-                const float* v = ix.base + (int64_t)id * d;
-                dist = expansion_from(qn, ix.base_norm[id], dot_seq(v, xq, d));
-            }
-            topk_offer(s, make_key(dist, (uint32_t)c), valid);
-            topk_round_end(s, SC_NT);
-        }
-        topk_finish(s);
-    }
-    for (int c = tid; c < a.k; c += SC_NT) {
-        a.out_ids[(int64_t)q * a.k + c] = c < kr ? cand[key_payload(best[c])] : -1;
-        a.out_dis[(int64_t)q * a.k + c] = c < kr ? key_dist(best[c]) : __int_as_float(0x7f800000);
-    }
+    scan_epilogue(ix, a, s, q, prefix, plist, cand, xq);
 }
 
 template <int M>

@@ -21,6 +21,8 @@ struct DevIndex {
     const float* coa_norm = nullptr;   // C   float norms (a-operand of the coarse product)
     const float* pq = nullptr;         // m x ks x ds
     const double* pq_norm = nullptr;   // m x ks double norms (b-operand of the table product)
+    const float* pq_hi = nullptr;      // m x ks  RN32(pq_norm)
+    const float* pq_lo = nullptr;      // m x ks  RN32(pq_norm - pq_hi)
     const int64_t* list_beg = nullptr; // C   first row of each list
     const int32_t* list_len = nullptr; // C
     const uint8_t* codes = nullptr;    // rows x m
@@ -39,6 +41,7 @@ struct ScanArgs {
     const int32_t* out_start = nullptr;// nq when SCAN_OUT_PACKED
     int32_t* out_ids = nullptr;
     float* out_dis = nullptr;
+    int* queue = nullptr;              // work counter of the persistent kernel (zeroed per launch)
 };
 
 // query norms: double accumulation of float squares (nn.c:137-142)
@@ -53,6 +56,11 @@ cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_
                                  float* coadis, cudaStream_t st);
 // fused residual + table + ADC scan + top-k (+ re-rank), one CTA per query
 cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
+
+// persistent register-codebook scan (d = 128, ks = 256, m in {4, 8, 16},
+// k or kl <= 1024); returns cudaErrorNotSupported when not applicable
+cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st);
+bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 
 // largest k / kl / w the scan kernel supports
 constexpr int MAX_K = 2048;

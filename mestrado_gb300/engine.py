@@ -19,7 +19,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import GBIVF_RERANK, GBIVF_TABLE_DIRECT, GbivfError, check  # noqa: F401
+from ._lib import GBIVF_PROFILE, GBIVF_RERANK, GBIVF_TABLE_DIRECT, GbivfError, check  # noqa: F401
 from .ivfdata import IVFPQData
 
 
@@ -81,24 +81,36 @@ class GpuIndex:
         return d.value, c.value, m.value, ks.value, n.value
 
     # -- searches ---------------------------------------------------------
-    def search(self, queries, k, w, kl=None, rerank=False, direct=False):
-        """ivfpq_search: (ids nq x k int32, dis nq x k float32)."""
+    def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None):
+        """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
+        pass preallocated (ids, dis) host arrays (e.g. pinned memory)."""
         q = _c(queries, np.float32)
         nq = q.shape[0]
-        ids = np.empty((nq, k), np.int32)
-        dis = np.empty((nq, k), np.float32)
+        if out is None:
+            ids = np.empty((nq, k), np.int32)
+            dis = np.empty((nq, k), np.float32)
+        else:
+            ids, dis = out
+            assert ids.shape == (nq, k) and ids.dtype == np.int32 and ids.flags.c_contiguous
+            assert dis.shape == (nq, k) and dis.dtype == np.float32 and dis.flags.c_contiguous
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
         return ids, dis
 
     def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      stream_ptr=0):
+                      stream_ptr=0, profile=False):
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
-        flags = GBIVF_RERANK if rerank else 0
+        flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
+
+    def last_stage_ms(self):
+        """(coarse_ms, scan_ms) of the last search made with profile=True."""
+        a, b = C.c_float(), C.c_float()
+        check(self.lib.gbivf_last_stage_ms(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def coarse_assign(self, queries, w):
         q = _c(queries, np.float32)
