@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -108,6 +109,7 @@ struct gbivf_index {
     int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
     int num_sms = 0;
     bool use_persistent = true;       // register-codebook scan where the shape allows
+    int scan_threads = 512;           // block size of the persistent scan (512 or 1024)
     std::vector<void*> owned;    // index allocations
     DBuf base, base_norm;
     cudaStream_t stream = nullptr;
@@ -206,6 +208,8 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         split_norm(pn[e], &phi[e], &plo[e]);
     }
     if (cudaDeviceGetAttribute(&ix->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) ix->num_sms = 1;
+    if (const char* v = getenv("GBIVF_SCAN_THREADS")) ix->scan_threads = atoi(v) == 1024 ? 1024 : 512;
+    if (const char* v = getenv("GBIVF_SCAN_KERNEL")) ix->use_persistent = strcmp(v, "general") != 0;
 
     DevIndex& dx = ix->dx;
     dx.d = d;
@@ -262,7 +266,7 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
     if (ix->use_persistent && scan_persistent_supported(ix->dx, a)) {
-        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, st));
+        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st));
     } else {
         CK(launch_scan(ix->dx, a, st));
     }

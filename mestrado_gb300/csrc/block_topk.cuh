@@ -7,30 +7,38 @@
 //
 //   * every thread offers keys; a key below the current k-th best is
 //     appended to the buffer (one shared atomic per warp, ballot-aggregated);
-//   * when the buffer could overflow on the next round, the block sorts it
-//     (bitonic network in shared memory) and merges it with the sorted best
-//     list (each element finds its output rank by binary search in the other
-//     list), keeping the k smallest; the threshold drops to the new k-th key.
+//   * a flush finds the exact k-th smallest key of (best u buffer) with a
+//     block radix select (8-bit digits, starting at the highest bit in which
+//     the pool's keys differ), keeps the keys <= it as the new best set
+//     (unordered) and lowers the threshold to it;
+//   * the final call sorts the k survivors (bitonic network).
 //
 // Keys are unique (the low 32 bits carry a unique payload), so the result is
 // exactly the k smallest keys, ascending.
 //
 // Protocol (all threads of the block, uniform control flow):
-//   topk_init(s, k)  ->  per round: offer() from every thread of every warp,
-//   then round_end(s, incoming) ...  ->  topk_finish(s)  -> best[0..nbest)
+//   topk_init(s, k)  ->  offer() from every thread of every warp, with
+//   topk_round_end(s, incoming) or explicit topk_flush(s, nb) between rounds
+//   ->  topk_finish(s)  ->  best[0..nbest) ascending
 #pragma once
 #include "common.cuh"
 
 namespace gbivf {
 
+constexpr int TOPK_WORK_BYTES = 256 * 4 + 8 * 4 + 4 * 8;  // histogram, ints, u64 slots
+
 struct TopKSmem {
-    u64* best;    // [kcap] sorted ascending, nbest valid
-    u64* tmp;     // [kcap] merge output
+    u64* best;    // [kcap] best set (unordered until topk_finish), nbest valid
+    u64* tmp;     // [kcap] compaction output
     u64* buf;     // [bcap] unsorted candidates, bcap a power of two
     int* nbuf;    // shared counters
     int* nbest;
     u64* thresh;  // current k-th best key (KEY_MAX until k are known)
     int k, kcap, bcap;
+    unsigned char* work;  // TOPK_WORK_BYTES, 8-byte aligned
+    __device__ int* hist() const { return reinterpret_cast<int*>(work); }
+    __device__ int* info() const { return reinterpret_cast<int*>(work + 1024); }
+    __device__ u64* slots() const { return reinterpret_cast<u64*>(work + 1056); }
 };
 
 __device__ __forceinline__ void topk_init(TopKSmem& s, int k) {
@@ -39,6 +47,8 @@ __device__ __forceinline__ void topk_init(TopKSmem& s, int k) {
         *s.nbuf = 0;
         *s.nbest = 0;
         *s.thresh = KEY_MAX;
+        s.slots()[0] = 0;
+        s.info()[4] = 0;
     }
     __syncthreads();
 }
@@ -56,14 +66,16 @@ __device__ __forceinline__ void topk_offer(TopKSmem& s, u64 key, bool valid) {
     if (pass) s.buf[base + __popc(mask & ((1u << lane) - 1u))] = key;
 }
 
-__device__ __forceinline__ int lower_bound_u64(const u64* a, int n, u64 x) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (a[mid] < x) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
+// Warp-collective append of keys that already passed the caller's filter.
+__device__ __forceinline__ void topk_push(TopKSmem& s, u64 key, bool pass) {
+    unsigned mask = __ballot_sync(0xffffffffu, pass);
+    if (mask == 0) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(s.nbuf, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pass) s.buf[base + __popc(mask & ((1u << lane) - 1u))] = key;
 }
 
 __device__ inline void bitonic_sort_smem(u64* a, int n) {
@@ -85,32 +97,129 @@ __device__ inline void bitonic_sort_smem(u64* a, int n) {
     }
 }
 
-// Merge the nb buffered keys into best. nb is the block-uniform count.
+// The K-th smallest (1-based) key of A[0..na) u B[0..nb), 1 <= K <= na+nb.
+// Expects slots()[0] == 0 on entry and leaves it 0.
+__device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B, int nb, int K) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+    int* hist = s.hist();
+    int* info = s.info();
+    u64* slot = s.slots();
+    const u64 ref = na > 0 ? A[0] : B[0];
+    u64 acc = 0;
+    for (int i = tid; i < na; i += nt) acc |= A[i] ^ ref;
+    for (int i = tid; i < nb; i += nt) acc |= B[i] ^ ref;
+    unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)acc);
+    unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(acc >> 32));
+    if (lane == 0 && (lo | hi)) atomicOr(&slot[0], ((u64)hi << 32) | lo);
+    __syncthreads();
+    const u64 diff = slot[0];
+    __syncthreads();
+    if (tid == 0) slot[0] = 0;
+    if (diff == 0) return ref;  // a single distinct key
+    int hib = 63 - __clzll((long long)diff);
+    u64 kmask = hib == 63 ? 0ull : (~0ull << (hib + 1));
+    u64 kval = ref & kmask;
+    int want = K;
+    for (;;) {
+        const int lob = max(hib - 7, 0);
+        const int width = hib - lob + 1;
+        const u64 dmask = ((1ull << width) - 1ull);
+        for (int i = tid; i < 256; i += nt) hist[i] = 0;
+        __syncthreads();
+        for (int i = tid; i < na; i += nt)
+            if ((A[i] & kmask) == kval) atomicAdd(&hist[(A[i] >> lob) & dmask], 1);
+        for (int i = tid; i < nb; i += nt)
+            if ((B[i] & kmask) == kval) atomicAdd(&hist[(B[i] >> lob) & dmask], 1);
+        __syncthreads();
+        if (tid < 32) {
+            // lane owns bins 8*lane .. 8*lane+7
+            int c[8], sum = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                c[j] = hist[8 * lane + j];
+                sum += c[j];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            int before = incl - sum;
+            if (before < want && want <= incl) {
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (before < want && want <= before + c[j]) {
+                        info[0] = 8 * lane + j;
+                        info[1] = want - before;
+                        info[2] = c[j];
+                    }
+                    before += c[j];
+                }
+            }
+        }
+        __syncthreads();
+        const int dig = info[0], cnt = info[2];
+        want = info[1];
+        __syncthreads();
+        kmask |= dmask << lob;
+        kval |= (u64)dig << lob;
+        if (lob == 0) return kval;  // all 64 bits known
+        if (cnt == 1) {
+            for (int i = tid; i < na; i += nt)
+                if ((A[i] & kmask) == kval) slot[1] = A[i];
+            for (int i = tid; i < nb; i += nt)
+                if ((B[i] & kmask) == kval) slot[1] = B[i];
+            __syncthreads();
+            const u64 r = slot[1];
+            __syncthreads();
+            return r;
+        }
+        hib = lob - 1;
+    }
+}
+
+// Merge the nb buffered keys into the best set. nb is block-uniform.
 __device__ inline void topk_flush(TopKSmem& s, int nb) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
     if (nb <= 0) return;
-    int n = 2;
-    while (n < nb) n <<= 1;
-    for (int i = nb + tid; i < n; i += nt) s.buf[i] = KEY_MAX;
-    __syncthreads();
-    bitonic_sort_smem(s.buf, n);
     const int na = *s.nbest, k = s.k;
-    for (int i = tid; i < na; i += nt) {
-        int r = i + lower_bound_u64(s.buf, nb, s.best[i]);
-        if (r < k) s.tmp[r] = s.best[i];
+    if (na + nb < k) {
+        for (int i = tid; i < nb; i += nt) s.best[na + i] = s.buf[i];
+        __syncthreads();
+        if (tid == 0) {
+            *s.nbest = na + nb;
+            *s.nbuf = 0;
+        }
+        __syncthreads();
+        return;
     }
-    for (int j = tid; j < nb; j += nt) {
-        int r = j + lower_bound_u64(s.best, na, s.buf[j]);
-        if (r < k) s.tmp[r] = s.buf[j];
+    const u64 T = block_kth(s, s.best, na, s.buf, nb, k);
+    int* ctr = s.info() + 4;  // zero on entry (topk_init / previous flush)
+    for (int i0 = 0; i0 < na + nb; i0 += nt) {
+        const int i = i0 + tid;
+        u64 x = 0;
+        bool keep = false;
+        if (i < na + nb) {
+            x = i < na ? s.best[i] : s.buf[i - na];
+            keep = x <= T;
+        }
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) {
+            int leader = __ffs(m) - 1, base = 0;
+            if (lane == leader) base = atomicAdd(ctr, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (keep) s.tmp[base + __popc(m & ((1u << lane) - 1u))] = x;
+        }
     }
     __syncthreads();
-    const int nn = min(k, na + nb);
-    for (int i = tid; i < nn; i += nt) s.best[i] = s.tmp[i];
+    for (int i = tid; i < k; i += nt) s.best[i] = s.tmp[i];
     __syncthreads();
     if (tid == 0) {
-        *s.nbest = nn;
+        *s.nbest = k;
         *s.nbuf = 0;
-        *s.thresh = (nn == k) ? s.best[k - 1] : KEY_MAX;
+        *s.thresh = T;
+        *ctr = 0;
     }
     __syncthreads();
 }
@@ -124,11 +233,20 @@ __device__ __forceinline__ void topk_round_end(TopKSmem& s, int incoming) {
     if (nb + incoming > s.bcap) topk_flush(s, nb);
 }
 
+// Final flush, then sort the survivors ascending.
 __device__ __forceinline__ void topk_finish(TopKSmem& s) {
     __syncthreads();
     int nb = *s.nbuf;
     __syncthreads();
     topk_flush(s, nb);
+    const int n = *s.nbest;
+    if (n > 1) {
+        int p = 2;
+        while (p < n) p <<= 1;
+        for (int i = n + threadIdx.x; i < p; i += blockDim.x) s.best[i] = KEY_MAX;
+        __syncthreads();
+        bitonic_sort_smem(s.best, p);
+    }
 }
 
 }  // namespace gbivf

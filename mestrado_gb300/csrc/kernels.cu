@@ -126,8 +126,9 @@ __global__ void __launch_bounds__(CS_NT) coarse_select_kernel(
     u64* tmp = best + kcap;
     u64* buf = tmp + kcap;
     u64* thresh = buf + bcap;
-    int* cnt = reinterpret_cast<int*>(thresh + 1);
-    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap};
+    unsigned char* work = reinterpret_cast<unsigned char*>(thresh + 1);
+    int* cnt = reinterpret_cast<int*>(work + TOPK_WORK_BYTES);
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, work};
     const int q = blockIdx.x, tid = threadIdx.x;
     const float* row = dist + (int64_t)q * C;
     topk_init(s, w);
@@ -154,7 +155,7 @@ cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_
     if (nq <= 0) return cudaSuccess;
     int kcap = pow2_at_least(std::max(w, 2));
     int bcap = pow2_at_least(std::max(2 * CS_NT * CS_ITEMS, kcap));
-    size_t sm = sizeof(u64) * (2 * kcap + bcap + 1) + 2 * sizeof(int);
+    size_t sm = sizeof(u64) * (2 * kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int);
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(coarse_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a
     int* plist = reinterpret_cast<int*>(smem + L.off_plist);
     int* cand = reinterpret_cast<int*>(smem + L.off_cand);
     int* cnt = reinterpret_cast<int*>(smem + L.off_cnt);
-    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap};
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, smem + L.off_work};
 
     const int q = blockIdx.x, tid = threadIdx.x;
     const int d = ix.d, m = ix.m, ks = ix.ks, ds = ix.ds, w = a.w;

@@ -59,7 +59,8 @@ cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
 
 // persistent register-codebook scan (d = 128, ks = 256, m in {4, 8, 16},
 // k or kl <= 1024); returns cudaErrorNotSupported when not applicable
-cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st);
+cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads,
+                                   cudaStream_t st);
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 
 // largest k / kl / w the scan kernel supports

@@ -11,10 +11,11 @@ namespace gbivf {
 
 struct ScanSmem {
     size_t off_best, off_tmp, off_buf, off_thresh, off_table, off_xq, off_r, off_rn, off_prefix,
-        off_plist, off_cand, off_cnt, off_misc, total;
+        off_plist, off_cand, off_cnt, off_misc, off_work, total;
 };
 
-inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap) {
+// tables: number of m x ks table buffers; rrows: residual rows held at once
+inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap, int tables = 1, int rrows = 1) {
     ScanSmem L;
     size_t o = 0;
     auto take = [&](size_t bytes, size_t align) {
@@ -27,15 +28,16 @@ inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap
     L.off_tmp = take(sizeof(u64) * kcap, 16);
     L.off_buf = take(sizeof(u64) * bcap, 16);
     L.off_thresh = take(sizeof(u64), 8);
-    L.off_table = take(sizeof(float) * m * ks, 16);
+    L.off_table = take(sizeof(float) * m * ks * tables, 16);
     L.off_xq = take(sizeof(float) * d, 16);
-    L.off_r = take(sizeof(float) * d, 16);
-    L.off_rn = take(sizeof(float) * m, 16);
+    L.off_r = take(sizeof(float) * d * rrows, 16);
+    L.off_rn = take(sizeof(float) * m * rrows, 16);
     L.off_prefix = take(sizeof(uint32_t) * (w + 1), 16);
     L.off_plist = take(sizeof(int) * w, 16);
     L.off_cand = take(sizeof(int) * kcap, 16);
     L.off_cnt = take(sizeof(int) * 2, 8);
     L.off_misc = take(sizeof(int) * 4, 8);
+    L.off_work = take(TOPK_WORK_BYTES, 16);
     L.total = (o + 15) / 16 * 16;
     return L;
 }
@@ -130,7 +132,20 @@ __device__ inline void scan_epilogue(const DevIndex& ix, const ScanArgs& a, TopK
             if (valid) {
                 const int32_t id = cand[c];
                 const float* v = ix.base + (int64_t)id * d;
-                dist = expansion_from(qn, ix.base_norm[id], dot_seq(v, xq, d));
+                float dot = 0.0f;
+                if ((d & 3) == 0) {  // rows are 16-byte aligned: vector loads, same order
+                    const float4* v4 = reinterpret_cast<const float4*>(v);
+                    for (int l = 0; l < d / 4; l++) {
+                        const float4 b = __ldg(v4 + l);
+                        dot = __fadd_rn(dot, __fmul_rn(b.x, xq[4 * l]));
+                        dot = __fadd_rn(dot, __fmul_rn(b.y, xq[4 * l + 1]));
+                        dot = __fadd_rn(dot, __fmul_rn(b.z, xq[4 * l + 2]));
+                        dot = __fadd_rn(dot, __fmul_rn(b.w, xq[4 * l + 3]));
+                    }
+                } else {
+                    dot = dot_seq(v, xq, d);
+                }
+                dist = expansion_from(qn, ix.base_norm[id], dot);
             }
             topk_offer(s, make_key(dist, (uint32_t)c), valid);
             topk_round_end(s, nt);

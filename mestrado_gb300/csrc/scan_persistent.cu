@@ -20,43 +20,48 @@
 #include "exact_round.cuh"
 #include "scan_common.cuh"
 
+
 namespace gbivf {
 
-constexpr int SP_NT = 512;
 constexpr int SP_UNROLL = 4;
 constexpr int SP_BCAP = 8192;   // candidate buffer (64 KB)
-constexpr int SP_EARLY = 2048;  // flush once this many are buffered before k are known
+constexpr int SP_SOFT = 2048;   // flush at a list boundary once this many are buffered
 
-template <int M, bool DIRECT>
-__global__ void __launch_bounds__(SP_NT, 1) ivf_scan_persistent_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap) {
-    constexpr int D = 128, KS = 256, DS = D / M, E = M * KS / SP_NT;
-    static_assert(E * SP_NT == M * KS, "entries must divide evenly");
+constexpr int SP_RCH = 16;  // residuals formed per chunk of probes
+
+template <int M, bool DIRECT, int NT>
+__global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap) {
+    constexpr int D = 128, KS = 256, DS = D / M, E = M * KS / NT;
+    constexpr int TPS = NT / M;  // threads per sub-quantizer
+    static_assert(E * NT == M * KS && E * TPS == KS, "entries must divide evenly");
     extern __shared__ __align__(16) unsigned char smem[];
     u64* best = reinterpret_cast<u64*>(smem + L.off_best);
     u64* tmp = reinterpret_cast<u64*>(smem + L.off_tmp);
     u64* buf = reinterpret_cast<u64*>(smem + L.off_buf);
     u64* thresh = reinterpret_cast<u64*>(smem + L.off_thresh);
-    float* table = reinterpret_cast<float*>(smem + L.off_table);
+    float* tables = reinterpret_cast<float*>(smem + L.off_table);  // 2 buffers
     float* xq = reinterpret_cast<float*>(smem + L.off_xq);
-    float* r = reinterpret_cast<float*>(smem + L.off_r);
-    float* rn = reinterpret_cast<float*>(smem + L.off_rn);
+    float* rr = reinterpret_cast<float*>(smem + L.off_r);    // SP_RCH x D residuals
+    float* rn = reinterpret_cast<float*>(smem + L.off_rn);   // SP_RCH x M sub-norms
     uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.off_prefix);
     int* plist = reinterpret_cast<int*>(smem + L.off_plist);
     int* cand = reinterpret_cast<int*>(smem + L.off_cand);
     int* cnt = reinterpret_cast<int*>(smem + L.off_cnt);
-    int* qslot = reinterpret_cast<int*>(smem + L.off_misc);
-    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, SP_BCAP};
+    int* qslot = reinterpret_cast<int*>(smem + L.off_misc);  // [0] current, [1] next
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, SP_BCAP, smem + L.off_work};
 
-    const int tid = threadIdx.x, w = a.w;
+    const int tid = threadIdx.x, lane = tid & 31, w = a.w;
     const bool src_res = a.flags & SCAN_SRC_RESIDUAL;
     const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
 
-    // this thread's slice of the codebook
+    // this thread's slice of the codebook: sub-quantizer my_s, centroids
+    // my_c0 .. my_c0+E-1 (consecutive, so the table row is one vector store)
+    const int my_s = tid / TPS, my_c0 = (tid % TPS) * E;
     float cen[E][DS];
     float nhi[E], nlo[E];
 #pragma unroll
     for (int i = 0; i < E; i++) {
-        const int e = tid + i * SP_NT;
+        const int e = my_s * KS + my_c0 + i;
         const float4* src = reinterpret_cast<const float4*>(ix.pq + (int64_t)e * DS);
 #pragma unroll
         for (int v = 0; v < DS / 4; v++) {
@@ -72,86 +77,152 @@ __global__ void __launch_bounds__(SP_NT, 1) ivf_scan_persistent_kernel(DevIndex 
         }
     }
 
+    if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);
     for (;;) {
-        if (tid == 0) *qslot = atomicAdd(a.queue, 1);
         __syncthreads();
-        const int q = *qslot;
+        const int q = qslot[1];
         if (q >= a.nq) break;
-        if (!src_res && tid < D) xq[tid] = a.queries[(int64_t)q * D + tid];
-        if (tid == 0) {
-            uint32_t acc = 0;
-            for (int j = 0; j < w; j++) {
-                int l = a.probes[(int64_t)q * w + j];
-                plist[j] = l;
-                prefix[j] = acc;
-                acc += (l >= 0) ? (uint32_t)ix.list_len[l] : 0u;
+        __syncthreads();
+        if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
+        if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
+        // probe lists and their prefix sums, one warp
+        if (tid < 32) {
+            uint32_t carry = 0;
+            for (int j0 = 0; j0 < w; j0 += 32) {
+                const int j = j0 + lane;
+                int l = -1;
+                uint32_t len = 0;
+                if (j < w) {
+                    l = __ldg(a.probes + (int64_t)q * w + j);
+                    len = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
+                    plist[j] = l;
+                }
+                uint32_t incl = len;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                if (j < w) prefix[j] = carry + incl - len;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
             }
-            prefix[w] = acc;
+            if (lane == 0) prefix[w] = carry;
         }
         topk_init(s, kk);
 
         for (int j = 0; j < w; j++) {
+            const int jr = j % SP_RCH;
+            if (jr == 0) {
+                // residuals of probes j .. j+SP_RCH-1 (bsxfunMINUS) and their
+                // sub-norms (the a-operand norm of compute_cross_distances)
+                const int nr = min(SP_RCH, w - j);
+                for (int e = tid; e < nr * D; e += NT) {
+                    const int p = e / D, x = e % D, l = plist[j + p];
+                    float v = 0.0f;
+                    if (l >= 0)
+                        v = src_res ? __ldg(a.residual + ((int64_t)q * w + j + p) * D + x)
+                                    : __fsub_rn(xq[x], __ldg(ix.coa + (int64_t)l * D + x));
+                    rr[p * D + x] = v;
+                }
+                __syncthreads();
+                if (!DIRECT)
+                    for (int e = tid; e < nr * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
+                __syncthreads();
+            }
             const int l = plist[j];
             if (l < 0) continue;
-            // 1. residual
-            if (tid < D)
-                r[tid] = src_res ? a.residual[((int64_t)q * w + j) * D + tid]
-                                 : __fsub_rn(xq[tid], ix.coa[(int64_t)l * D + tid]);
-            __syncthreads();
-            // 2. sub-norms; everyone reads the buffer count (all appends of the
-            //    previous list happened before the barrier above)
-            if (!DIRECT && tid < M) rn[tid] = norm_f_seq(r + tid * DS, DS);
-            const int nb = *s.nbuf;
-            __syncthreads();
-            // 3. table from the register codebook
+            float* table = tables + (j & 1) * (M * KS);
+            // table row segment from the register codebook
+            {
+                float rs[DS];
+                const float4* r4 = reinterpret_cast<const float4*>(rr + jr * D + my_s * DS);
 #pragma unroll
-            for (int i = 0; i < E; i++) {
-                const int e = tid + i * SP_NT;
-                const int sq = e / KS;
-                const float* rs = r + sq * DS;
-                float v;
-                if (DIRECT) {
-                    v = 0.0f;
-#pragma unroll
-                    for (int t = 0; t < DS; t++) {
-                        float df = __fsub_rn(rs[t], cen[i][t]);
-                        v = __fadd_rn(v, __fmul_rn(df, df));
-                    }
-                } else {
-                    float dot = 0.0f;
-#pragma unroll
-                    for (int t = 0; t < DS; t++) dot = __fadd_rn(dot, __fmul_rn(rs[t], cen[i][t]));
-                    const float c0 = add_norms_rn(ix.pq_norm + e, nhi[i], nlo[i], rn[sq]);
-                    v = __fadd_rn(__fmul_rn(-2.0f, dot), c0);
+                for (int v4 = 0; v4 < DS / 4; v4++) {
+                    const float4 x = r4[v4];
+                    rs[4 * v4] = x.x;
+                    rs[4 * v4 + 1] = x.y;
+                    rs[4 * v4 + 2] = x.z;
+                    rs[4 * v4 + 3] = x.w;
                 }
-                table[e] = v;
+                const float f = DIRECT ? 0.0f : rn[jr * M + my_s];
+                float out[E];
+#pragma unroll
+                for (int i = 0; i < E; i++) {
+                    if (DIRECT) {
+                        float v = 0.0f;
+#pragma unroll
+                        for (int t = 0; t < DS; t++) {
+                            float df = __fsub_rn(rs[t], cen[i][t]);
+                            v = __fadd_rn(v, __fmul_rn(df, df));
+                        }
+                        out[i] = v;
+                    } else {
+                        float dot = 0.0f;
+#pragma unroll
+                        for (int t = 0; t < DS; t++) dot = __fadd_rn(dot, __fmul_rn(rs[t], cen[i][t]));
+                        const int e = my_s * KS + my_c0 + i;
+                        const float c0 = add_norms_rn(ix.pq_norm + e, nhi[i], nlo[i], f);
+                        out[i] = __fadd_rn(__fmul_rn(-2.0f, dot), c0);
+                    }
+                }
+                float* dst = table + my_s * KS + my_c0;
+                if constexpr (E % 4 == 0) {
+#pragma unroll
+                    for (int i = 0; i < E; i += 4)
+                        *reinterpret_cast<float4*>(dst + i) = make_float4(out[i], out[i + 1], out[i + 2], out[i + 3]);
+                } else if constexpr (E % 2 == 0) {
+#pragma unroll
+                    for (int i = 0; i < E; i += 2) *reinterpret_cast<float2*>(dst + i) = make_float2(out[i], out[i + 1]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < E; i++) dst[i] = out[i];
+                }
             }
             const int len = ix.list_len[l];
-            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kk && nb >= SP_EARLY);
+            // all appends of the previous list are done at this barrier; the
+            // count is read between it and the next one, before new appends
+            __syncthreads();
+            const int nb = *s.nbuf;
+            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kk && nb >= kk) || nb >= SP_SOFT;
             __syncthreads();
             if (flush_now) topk_flush(s, nb);
-            // 4. ADC scan of the list
+            // ADC scan of the list; the filter compares floats first
             const uint8_t* codes = ix.codes + ix.list_beg[l] * (int64_t)M;
             const uint32_t pos0 = prefix[j];
             const bool fits = len <= SP_BCAP - (flush_now ? 0 : nb);
-            for (int i0 = 0; i0 < len; i0 += SP_NT * SP_UNROLL) {
+            u64 tk = *s.thresh;
+            float td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
+            uint32_t tp = key_payload(tk);
+            const int full = fits ? len / (NT * SP_UNROLL) * (NT * SP_UNROLL) : 0;
+            for (int i0 = 0; i0 < full; i0 += NT * SP_UNROLL) {
                 float dist[SP_UNROLL];
 #pragma unroll
-                for (int u = 0; u < SP_UNROLL; u++) {
-                    const int i = i0 + u * SP_NT + tid;
-                    dist[u] = i < len ? adc_row<M>(codes + (int64_t)i * M, table, M, KS) : 0.0f;
-                }
+                for (int u = 0; u < SP_UNROLL; u++)
+                    dist[u] = adc_row<M>(codes + (int64_t)(i0 + u * NT + tid) * M, table, M, KS);
 #pragma unroll
                 for (int u = 0; u < SP_UNROLL; u++) {
-                    const int i = i0 + u * SP_NT + tid;
-                    topk_offer(s, make_key(dist[u], pos0 + (uint32_t)i), i < len);
+                    const uint32_t pos = pos0 + (uint32_t)(i0 + u * NT + tid);
+                    const bool pass = dist[u] < td || (dist[u] == td && pos < tp);
+                    topk_push(s, make_key(dist[u], pos), pass);
                 }
-                if (!fits) topk_round_end(s, SP_NT * SP_UNROLL);
+            }
+            for (int i0 = full; i0 < len; i0 += NT) {
+                const int i = i0 + tid;
+                const bool valid = i < len;
+                const float dist = valid ? adc_row<M>(codes + (int64_t)i * M, table, M, KS) : 0.0f;
+                const uint32_t pos = pos0 + (uint32_t)i;
+                const bool pass = valid && (dist < td || (dist == td && pos < tp));
+                topk_push(s, make_key(dist, pos), pass);
+                if (!fits) {
+                    topk_round_end(s, NT);
+                    tk = *s.thresh;
+                    td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
+                    tp = key_payload(tk);
+                }
             }
         }
         topk_finish(s);
         scan_epilogue(ix, a, s, q, prefix, plist, cand, xq);
-        __syncthreads();
     }
 }
 
@@ -162,34 +233,40 @@ bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
            ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK));
 }
 
-template <int M, bool DIRECT>
+template <int M, bool DIRECT, int NT>
 static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
     const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
     const int kcap = pow2_at_least(std::max(std::max(kk, a.k), 2));
-    ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP);
-    auto kern = ivf_scan_persistent_kernel<M, DIRECT>;
+    ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH);
+    auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SP_NT, L.total);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, L.total);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int grid = std::min(a.nq, num_sms * per_sm);
     e = cudaMemsetAsync(a.queue, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    kern<<<grid, SP_NT, L.total, st>>>(ix, a, L, kcap);
+    kern<<<grid, NT, L.total, st>>>(ix, a, L, kcap);
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
-    if (a.nq <= 0) return cudaSuccess;
-    if (!scan_persistent_supported(ix, a)) return cudaErrorNotSupported;
+template <int NT>
+static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
     const bool direct = a.flags & SCAN_TABLE_DIRECT;
     switch (ix.m) {
-        case 4: return direct ? launch_sp<4, true>(ix, a, num_sms, st) : launch_sp<4, false>(ix, a, num_sms, st);
-        case 8: return direct ? launch_sp<8, true>(ix, a, num_sms, st) : launch_sp<8, false>(ix, a, num_sms, st);
-        default: return direct ? launch_sp<16, true>(ix, a, num_sms, st) : launch_sp<16, false>(ix, a, num_sms, st);
+        case 4: return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st) : launch_sp<4, false, NT>(ix, a, num_sms, st);
+        case 8: return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st) : launch_sp<8, false, NT>(ix, a, num_sms, st);
+        default:
+            return direct ? launch_sp<16, true, NT>(ix, a, num_sms, st) : launch_sp<16, false, NT>(ix, a, num_sms, st);
     }
+}
+
+cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads, cudaStream_t st) {
+    if (a.nq <= 0) return cudaSuccess;
+    if (!scan_persistent_supported(ix, a)) return cudaErrorNotSupported;
+    return threads == 1024 ? launch_sp_nt<1024>(ix, a, num_sms, st) : launch_sp_nt<512>(ix, a, num_sms, st);
 }
 
 }  // namespace gbivf
