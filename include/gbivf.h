@@ -110,6 +110,25 @@ int gbivf_last_stage_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms);
 int gbivf_coarse_assign(gbivf_index *ix, const float *queries, int nq, int w, int32_t *coaidx,
                         float *coadis);
 
+/* Size of the device scratch array behind gbivf_coarse_assign_noalloc. */
+#define GBIVF_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* The coarse stage for callers that cannot allocate device memory (a host
+ * that gives plugins a fixed device-memory budget and forbids allocation, or
+ * a serving loop that must not take cudaMalloc's device-wide
+ * synchronisation). Same results as gbivf_coarse_assign, on device buffers:
+ * d_queries nq x d, d_coaidx / d_coadis nq x w, enqueued on `stream`
+ * (a cudaStream_t, NULL = default stream); returns after launching. It
+ * allocates nothing: its scratch is one file-scope device array of
+ * GBIVF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit, so nq * (8 + 4 * coarsek) plus alignment must fit in it (larger
+ * calls return GBIVF_ERR_UNSUPPORTED; split the batch). The first call on a
+ * device looks up the array's address (cudaGetSymbolAddress), so make it
+ * before any stream capture. Calls that overlap on the GPU share the array
+ * and race. No counterpart in the reference. */
+int gbivf_coarse_assign_noalloc(gbivf_index *ix, const float *d_queries, int nq, int w,
+                                int32_t *d_coaidx, float *d_coadis, void *stream);
+
 /* core_gpu(PQ, residual, ivf, ivf_size, rid_to_ivf, qid_to_starting_outid,
  * idxs, dists, k, w) (parallel2/ivf_pq/mycuda.cu:119-188): residual is
  * nres x d (nres = nq*w), list rid_to_ivf[r] for residual r; tables are the

@@ -22,7 +22,7 @@ EXPORTS = [
     "gbivf_last_error", "gbivf_version", "gbivf_index_create", "gbivf_index_create_from_lists",
     "gbivf_index_set_base", "gbivf_index_destroy", "gbivf_index_dims", "gbivf_ivfpq_search",
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
-    "gbivf_pq_search", "gbivf_last_stage_ms",
+    "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc",
 ]
 
 
@@ -58,6 +58,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_pq_create.argtypes = [C.POINTER(vp), i32, i32, i32, i32, vp, vp, i64]
     lib.gbivf_pq_search.argtypes = [vp, vp, i32, i32, vp, vp]
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
+    lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
     for name in EXPORTS:
         if name != "gbivf_last_error":
             getattr(lib, name).restype = i32

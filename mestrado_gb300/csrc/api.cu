@@ -594,3 +594,69 @@ int gbivf_pq_search(gbivf_index* ix, const float* queries, int nq, int k, float*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Coarse assignment without device allocation.
+//
+// Some callers cannot call cudaMalloc: a host that hands its plugins a fixed
+// device-memory budget and forbids them to allocate, or a serving loop that
+// must not take the allocator's device-wide synchronisation on its latency
+// path. For them the coarse stage's scratch (query norms and the query x
+// centroid distance block) lives in one file-scope device array of
+// GBIVF_NOALLOC_SCRATCH_BYTES. Every GPU that loads this library holds the
+// array until the process exits. The host resolves the array's device address
+// with cudaGetSymbolAddress once per device, on the first call made on that
+// device (so that first call should come before any stream capture).
+// All calls share the array: calls that overlap on the GPU (other streams,
+// other threads) race on it. The kernels overwrite every scratch byte they
+// read, so nothing needs clearing between calls.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t kNoallocScratchBytes = (size_t)GBIVF_NOALLOC_SCRATCH_BYTES;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[128] = {};
+
+}  // namespace
+
+extern "C" int gbivf_coarse_assign_noalloc(gbivf_index* ix, const float* d_queries, int nq, int w, int32_t* d_coaidx,
+                                           float* d_coadis, void* stream) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
+    if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    if (nq == 0) return GBIVF_OK;
+    if (!d_queries || !d_coaidx || !d_coadis) return fail(GBIVF_ERR_INVALID, "NULL device buffer");
+    const DevIndex& dx = ix->dx;
+    const size_t norm_bytes = ((size_t)nq * sizeof(double) + 255) / 256 * 256;
+    const size_t need = norm_bytes + (size_t)nq * dx.C * sizeof(float);
+    if (need > kNoallocScratchBytes)
+        return fail(GBIVF_ERR_UNSUPPORTED,
+                    "nq=%d with coarsek=%d needs %zu scratch bytes; the no-allocation scratch holds %zu "
+                    "(at most %zu queries per call at this coarsek)",
+                    nq, dx.C, need, kNoallocScratchBytes,
+                    (kNoallocScratchBytes - 256) / (sizeof(double) + (size_t)dx.C * sizeof(float)));
+    if (ix->device < 0 || ix->device >= 128) return fail(GBIVF_ERR_UNSUPPORTED, "device %d", ix->device);
+    DeviceGuard g(ix->device);
+    if (!g.ok) return fail(GBIVF_ERR_CUDA, "cudaSetDevice(%d) failed", ix->device);
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[ix->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+            g_noalloc_ptr[ix->device] = p;
+        }
+        base = g_noalloc_ptr[ix->device];
+    }
+    double* qn = reinterpret_cast<double*>(base);
+    float* dist = reinterpret_cast<float*>(static_cast<unsigned char*>(base) + norm_bytes);
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(launch_norm_d(d_queries, nq, dx.d, qn, st));
+    CK(launch_coarse_dist(dx, d_queries, qn, nq, dist, st));
+    CK(launch_coarse_select(dist, nq, dx.C, w, d_coaidx, d_coadis, st));
+    return GBIVF_OK;
+}
