@@ -115,7 +115,7 @@ struct gbivf_index {
     cudaStream_t stream = nullptr;
     std::mutex mu;
     // workspace
-    DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue;
+    DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue, w_ckey, w_cid, w_ccnt;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
     bool ev_valid = false;
 };
@@ -137,7 +137,8 @@ void free_index(gbivf_index* ix) {
     for (void* p : ix->owned) cudaFree(p);
     ix->owned.clear();
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
-                    &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue})
+                    &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
+                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -266,6 +267,14 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
     if (ix->use_persistent && scan_persistent_supported(ix->dx, a)) {
+        const int stride = scan_persistent_stride(a);
+        CK(ix->w_ckey.ensure(sizeof(unsigned long long) * (size_t)a.nq * stride));
+        CK(ix->w_cid.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
+        CK(ix->w_ccnt.ensure(sizeof(int32_t) * (size_t)a.nq));
+        a.cand_key = ix->w_ckey.as<unsigned long long>();
+        a.cand_id = ix->w_cid.as<int32_t>();
+        a.cand_cnt = ix->w_ccnt.as<int32_t>();
+        a.cand_stride = stride;
         CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st));
     } else {
         CK(launch_scan(ix->dx, a, st));

@@ -42,6 +42,12 @@ struct ScanArgs {
     int32_t* out_ids = nullptr;
     float* out_dis = nullptr;
     int* queue = nullptr;              // work counter of the persistent kernel (zeroed per launch)
+    // hand-off from the persistent scan to its finalize kernel: per query the
+    // unsorted best keys and their base ids (cand_stride slots) and a count
+    unsigned long long* cand_key = nullptr;
+    int32_t* cand_id = nullptr;
+    int32_t* cand_cnt = nullptr;
+    int cand_stride = 0;
 };
 
 // query norms: double accumulation of float squares (nn.c:137-142)
@@ -62,6 +68,8 @@ cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
 cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads,
                                    cudaStream_t st);
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
+// candidate slots per query the persistent scan needs in ScanArgs::cand_*
+int scan_persistent_stride(const ScanArgs& a);
 
 // largest k / kl / w the scan kernel supports
 constexpr int MAX_K = 2048;

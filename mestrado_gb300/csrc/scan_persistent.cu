@@ -23,16 +23,40 @@
 
 namespace gbivf {
 
-constexpr int SP_UNROLL = 4;
 constexpr int SP_BCAP = 8192;   // candidate buffer (64 KB)
 constexpr int SP_SOFT = 2048;   // flush at a list boundary once this many are buffered
+constexpr int SP_RCH = 16;      // residuals formed per chunk of probes
 
-constexpr int SP_RCH = 16;  // residuals formed per chunk of probes
+// one code row as a vector load
+template <int M> struct CodeRow;
+template <> struct CodeRow<4> { using T = uint32_t; };
+template <> struct CodeRow<8> { using T = uint2; };
+template <> struct CodeRow<16> { using T = uint4; };
+
+template <int M>
+__device__ __forceinline__ typename CodeRow<M>::T load_row(const uint8_t* p) {
+    return __ldg(reinterpret_cast<const typename CodeRow<M>::T*>(p));
+}
+
+__device__ __forceinline__ float adc4(float acc, uint32_t v, const float* T) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * 256 + ((v >> (8 * s)) & 0xff)]);
+    return acc;
+}
+
+// acc = 0; acc += T[s][code[s]] in s order (sumidxtab2, ivf_search.cpp:189-200)
+__device__ __forceinline__ float adc_sum(uint32_t v, const float* T) { return adc4(0.0f, v, T); }
+__device__ __forceinline__ float adc_sum(uint2 v, const float* T) { return adc4(adc4(0.0f, v.x, T), v.y, T + 1024); }
+__device__ __forceinline__ float adc_sum(uint4 v, const float* T) {
+    return adc4(adc4(adc4(adc4(0.0f, v.x, T), v.y, T + 1024), v.z, T + 2048), v.w, T + 3072);
+}
 
 template <int M, bool DIRECT, int NT>
 __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap) {
     constexpr int D = 128, KS = 256, DS = D / M, E = M * KS / NT;
     constexpr int TPS = NT / M;  // threads per sub-quantizer
+    constexpr int U = M >= 16 ? 2 : 4;
+    using CT = typename CodeRow<M>::T;
     static_assert(E * NT == M * KS && E * TPS == KS, "entries must divide evenly");
     extern __shared__ __align__(16) unsigned char smem[];
     u64* best = reinterpret_cast<u64*>(smem + L.off_best);
@@ -45,9 +69,8 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     float* rn = reinterpret_cast<float*>(smem + L.off_rn);   // SP_RCH x M sub-norms
     uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.off_prefix);
     int* plist = reinterpret_cast<int*>(smem + L.off_plist);
-    int* cand = reinterpret_cast<int*>(smem + L.off_cand);
     int* cnt = reinterpret_cast<int*>(smem + L.off_cnt);
-    int* qslot = reinterpret_cast<int*>(smem + L.off_misc);  // [0] current, [1] next
+    int* qslot = reinterpret_cast<int*>(smem + L.off_misc);  // [1] = next query
     TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, SP_BCAP, smem + L.off_work};
 
     const int tid = threadIdx.x, lane = tid & 31, w = a.w;
@@ -131,6 +154,15 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             }
             const int l = plist[j];
             if (l < 0) continue;
+            const int len = __ldg(ix.list_len + l);
+            const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
+            // first chunk of codes in flight during the table build
+            CT cur[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int i = u * NT + tid;
+                cur[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+            }
             float* table = tables + (j & 1) * (M * KS);
             // table row segment from the register codebook
             {
@@ -178,7 +210,6 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     for (int i = 0; i < E; i++) dst[i] = out[i];
                 }
             }
-            const int len = ix.list_len[l];
             // all appends of the previous list are done at this barrier; the
             // count is read between it and the next one, before new appends
             __syncthreads();
@@ -186,43 +217,146 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kk && nb >= kk) || nb >= SP_SOFT;
             __syncthreads();
             if (flush_now) topk_flush(s, nb);
-            // ADC scan of the list; the filter compares floats first
-            const uint8_t* codes = ix.codes + ix.list_beg[l] * (int64_t)M;
+            // ADC scan of the list, software-pipelined one chunk ahead; the
+            // filter compares floats first; warps past the end skip the chunk
             const uint32_t pos0 = prefix[j];
             const bool fits = len <= SP_BCAP - (flush_now ? 0 : nb);
             u64 tk = *s.thresh;
             float td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
             uint32_t tp = key_payload(tk);
-            const int full = fits ? len / (NT * SP_UNROLL) * (NT * SP_UNROLL) : 0;
-            for (int i0 = 0; i0 < full; i0 += NT * SP_UNROLL) {
-                float dist[SP_UNROLL];
+            for (int i0 = 0; i0 < len; i0 += NT * U) {
+                CT nxt[U];
 #pragma unroll
-                for (int u = 0; u < SP_UNROLL; u++)
-                    dist[u] = adc_row<M>(codes + (int64_t)(i0 + u * NT + tid) * M, table, M, KS);
-#pragma unroll
-                for (int u = 0; u < SP_UNROLL; u++) {
-                    const uint32_t pos = pos0 + (uint32_t)(i0 + u * NT + tid);
-                    const bool pass = dist[u] < td || (dist[u] == td && pos < tp);
-                    topk_push(s, make_key(dist[u], pos), pass);
+                for (int u = 0; u < U; u++) {
+                    const int i = i0 + NT * U + u * NT + tid;
+                    nxt[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
                 }
-            }
-            for (int i0 = full; i0 < len; i0 += NT) {
-                const int i = i0 + tid;
-                const bool valid = i < len;
-                const float dist = valid ? adc_row<M>(codes + (int64_t)i * M, table, M, KS) : 0.0f;
-                const uint32_t pos = pos0 + (uint32_t)i;
-                const bool pass = valid && (dist < td || (dist == td && pos < tp));
-                topk_push(s, make_key(dist, pos), pass);
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int iw = i0 + u * NT + (tid & ~31);
+                    if (iw < len) {
+                        const int i = i0 + u * NT + tid;
+                        const float dist = adc_sum(cur[u], table);
+                        const uint32_t pos = pos0 + (uint32_t)i;
+                        const bool pass = i < len && (dist < td || (dist == td && pos < tp));
+                        topk_push(s, make_key(dist, pos), pass);
+                    }
+                }
                 if (!fits) {
-                    topk_round_end(s, NT);
+                    topk_round_end(s, NT * U);
                     tk = *s.thresh;
                     td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
                     tp = key_payload(tk);
                 }
+#pragma unroll
+                for (int u = 0; u < U; u++) cur[u] = nxt[u];
             }
         }
-        topk_finish(s);
-        scan_epilogue(ix, a, s, q, prefix, plist, cand, xq);
+        // final merge; hand the unsorted best set (keys and base ids) over
+        {
+            __syncthreads();
+            const int nb = *s.nbuf;
+            __syncthreads();
+            topk_flush(s, nb);
+        }
+        const int nbest = *s.nbest;
+        for (int c = tid; c < a.cand_stride; c += NT) {
+            const int64_t o = (int64_t)q * a.cand_stride + c;
+            if (c < nbest) {
+                a.cand_key[o] = best[c];
+                a.cand_id[o] = pos_to_id(ix, prefix, plist, w, key_payload(best[c]));
+            } else {
+                a.cand_key[o] = KEY_MAX;
+                a.cand_id[o] = -1;
+            }
+        }
+        if (tid == 0) a.cand_cnt[q] = nbest;
+    }
+}
+
+// Per query (one CTA): sort the hand-off set, then write it, or re-rank it by
+// exact L2 (ivf_search.cpp:113-134) and write the k best.
+constexpr int FIN_NT = 128;
+
+__device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = tid; i < (n >> 1); i += nt) {
+                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const u64 x = a[lo], y = a[hi];
+                if ((x > y) == asc) {
+                    a[lo] = y;
+                    a[hi] = x;
+                    const int32_t t = b[lo];
+                    b[lo] = b[hi];
+                    b[hi] = t;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int n2 = a.cand_stride;  // power of two
+    u64* keys = reinterpret_cast<u64*>(fsm);
+    int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
+    float* xq = reinterpret_cast<float*>(ids + n2);
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const int n = a.cand_cnt[q];
+    for (int c = tid; c < n2; c += FIN_NT) {
+        keys[c] = a.cand_key[(int64_t)q * n2 + c];
+        ids[c] = a.cand_id[(int64_t)q * n2 + c];
+    }
+    const bool rerank = a.flags & SCAN_RERANK;
+    if (rerank)
+        for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
+    __syncthreads();
+    bitonic_sort_pairs(keys, ids, n2);
+    const float inf = __int_as_float(0x7f800000);
+    if (!rerank) {
+        if (a.flags & SCAN_OUT_PACKED) {
+            const int64_t o = a.out_start[q];
+            for (int c = tid; c < n; c += FIN_NT) {
+                a.out_ids[o + c] = ids[c];
+                a.out_dis[o + c] = key_dist(keys[c]);
+            }
+        } else {
+            for (int c = tid; c < a.k; c += FIN_NT) {
+                a.out_ids[(int64_t)q * a.k + c] = c < n ? ids[c] : -1;
+                a.out_dis[(int64_t)q * a.k + c] = c < n ? key_dist(keys[c]) : inf;
+            }
+        }
+        return;
+    }
+    // exact distances of the n candidates in ADC order, keyed by that rank
+    const double qn = a.qnorm[q];
+    const int d = ix.d;
+    for (int c = tid; c < n2; c += FIN_NT) {
+        u64 key = KEY_MAX;
+        if (c < n) {
+            const float4* v4 = reinterpret_cast<const float4*>(ix.base + (int64_t)ids[c] * d);
+            float dot = 0.0f;
+            for (int l = 0; l < d / 4; l++) {
+                const float4 b = __ldg(v4 + l);
+                dot = __fadd_rn(dot, __fmul_rn(b.x, xq[4 * l]));
+                dot = __fadd_rn(dot, __fmul_rn(b.y, xq[4 * l + 1]));
+                dot = __fadd_rn(dot, __fmul_rn(b.z, xq[4 * l + 2]));
+                dot = __fadd_rn(dot, __fmul_rn(b.w, xq[4 * l + 3]));
+            }
+            key = make_key(expansion_from(qn, ix.base_norm[ids[c]], dot), (uint32_t)c);
+        }
+        keys[c] = key;
+    }
+    __syncthreads();
+    bitonic_sort_smem(keys, n2);
+    const int kr = min(a.k, n);
+    for (int c = tid; c < a.k; c += FIN_NT) {
+        a.out_ids[(int64_t)q * a.k + c] = c < kr ? ids[key_payload(keys[c])] : -1;
+        a.out_dis[(int64_t)q * a.k + c] = c < kr ? key_dist(keys[c]) : inf;
     }
 }
 
@@ -233,10 +367,15 @@ bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
            ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK));
 }
 
+int scan_persistent_stride(const ScanArgs& a) {
+    const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
+    return pow2_at_least(std::max(std::max(kk, a.k), 2));
+}
+
 template <int M, bool DIRECT, int NT>
 static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
-    const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
-    const int kcap = pow2_at_least(std::max(std::max(kk, a.k), 2));
+    const int kcap = scan_persistent_stride(a);
+    if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
     ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH);
     auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
@@ -249,6 +388,14 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
     e = cudaMemsetAsync(a.queue, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     kern<<<grid, NT, L.total, st>>>(ix, a, L, kcap);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const size_t fsm = (size_t)kcap * (sizeof(u64) + sizeof(int32_t)) + sizeof(float) * 128;
+    if (fsm > 48 * 1024) {
+        e = cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+        if (e != cudaSuccess) return e;
+    }
+    finalize_kernel<<<a.nq, FIN_NT, fsm, st>>>(ix, a);
     return cudaGetLastError();
 }
 
