@@ -20,6 +20,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libgbivf.so")
+# C++ shims with the reference's own signatures, linked against libgbivf.so
+SHIMS = {"libgbivf_refcompat_seq.so": "refcompat_seq.cpp", "libgbivf_refcompat_par2.so": "refcompat_par2.cpp"}
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["kernels.cu", "scan_persistent.cu", "api.cu"]
@@ -39,8 +41,8 @@ def nvcc() -> str:
 
 
 def _deps() -> list[str]:
-    out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
-    out.append(os.path.join(INCLUDE, "gbivf.h"))
+    out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
+    out += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     out.append(os.path.abspath(__file__))
     return out
 
@@ -54,8 +56,9 @@ def _compile(src: str, obj: str, extra: list[str]) -> None:
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
+    outs = [LIB] + [os.path.join(LIBDIR, n) for n in SHIMS]
+    if not force and all(os.path.exists(o) for o in outs):
+        t = min(os.path.getmtime(o) for o in outs)
         if all(os.path.getmtime(p) <= t for p in _deps()):
             return LIB
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
@@ -68,6 +71,15 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    for name, src in SHIMS.items():
+        out = os.path.join(LIBDIR, name)
+        tmp = out + f".tmp{os.getpid()}"
+        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", INCLUDE, "-o", tmp, os.path.join(CSRC, src),
+               "-L", LIBDIR, "-lgbivf", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"shim build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, out)
     return LIB
 
 
