@@ -40,7 +40,10 @@ extern "C" {
 /* search flags */
 #define GBIVF_RERANK 0x1u       /* exact L2 re-rank of the kl ADC candidates to k */
 #define GBIVF_TABLE_DIRECT 0x2u /* tables as sum (r-c)^2 (parallel2) instead of the expansion */
+#define GBIVF_MIXED_COARSE 0x4u /* coarse stage as a BF16 tensor-core GEMM + exact FP32 re-check (d = 128);
+                                   the probed lists are identical to the plain path's */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
+#define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
 typedef struct gbivf_index gbivf_index;
 
@@ -128,6 +131,12 @@ int gbivf_coarse_assign(gbivf_index *ix, const float *queries, int nq, int w, in
  * and race. No counterpart in the reference. */
 int gbivf_coarse_assign_noalloc(gbivf_index *ix, const float *d_queries, int nq, int w,
                                 int32_t *d_coaidx, float *d_coadis, void *stream);
+
+/* gbivf_coarse_assign with search flags (GBIVF_MIXED_COARSE selects the
+ * tensor-core form). `ncand`, when not NULL, receives the number of
+ * centroids the mixed form re-checked exactly (0 for the plain form). */
+int gbivf_coarse_assign_flags(gbivf_index *ix, const float *queries, int nq, int w, unsigned flags,
+                              int32_t *coaidx, float *coadis, int64_t *ncand);
 
 /* core_gpu(PQ, residual, ivf, ivf_size, rid_to_ivf, qid_to_starting_outid,
  * idxs, dists, k, w) (parallel2/ivf_pq/mycuda.cu:119-188): residual is

@@ -13,6 +13,7 @@ from . import build as _build
 GBIVF_OK = 0
 GBIVF_RERANK = 0x1
 GBIVF_TABLE_DIRECT = 0x2
+GBIVF_MIXED_COARSE = 0x4
 GBIVF_PROFILE = 0x100
 
 _lib = None
@@ -22,7 +23,7 @@ EXPORTS = [
     "gbivf_last_error", "gbivf_version", "gbivf_index_create", "gbivf_index_create_from_lists",
     "gbivf_index_set_base", "gbivf_index_destroy", "gbivf_index_dims", "gbivf_ivfpq_search",
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
-    "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc",
+    "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc", "gbivf_coarse_assign_flags",
 ]
 
 
@@ -59,6 +60,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_pq_search.argtypes = [vp, vp, i32, i32, vp, vp]
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
+    lib.gbivf_coarse_assign_flags.argtypes = [vp, vp, i32, i32, u32, vp, vp, vp]
     for name in EXPORTS:
         if name != "gbivf_last_error":
             getattr(lib, name).restype = i32

@@ -108,6 +108,8 @@ struct gbivf_index {
     std::vector<int32_t> h_len;  // list sizes (host copy)
     int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
     int num_sms = 0;
+    bool mixed_pending = false;       // a mixed coarse stage ran since the last flag check
+    int64_t last_ncand = 0;
     bool use_persistent = true;       // register-codebook scan where the shape allows
     int scan_threads = 512;           // block size of the persistent scan (512 or 1024)
     std::vector<void*> owned;    // index allocations
@@ -116,6 +118,8 @@ struct gbivf_index {
     std::mutex mu;
     // workspace
     DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue, w_ckey, w_cid, w_ccnt;
+    // mixed-precision coarse stage: centroid BF16 tiles, centroid lengths, query tiles, flags
+    DBuf coa_tiles, coa_len, w_qtiles, w_flags;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
     bool ev_valid = false;
 };
@@ -138,7 +142,7 @@ void free_index(gbivf_index* ix) {
     ix->owned.clear();
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
-                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt})
+                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->w_qtiles, &ix->w_flags})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -288,7 +292,10 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (k <= 0 || k > MAX_K) return fail(k <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "k=%d (1..%d)", k, MAX_K);
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
-    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE))
+        return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
     if (flags & GBIVF_RERANK) {
         if (kl <= 0 || kl > MAX_K) return fail(kl <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "kl=%d (1..%d)", kl, MAX_K);
         if (!ix->base.p) return fail(GBIVF_ERR_INVALID, "GBIVF_RERANK needs gbivf_index_set_base first");
@@ -296,6 +303,71 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
             return fail(GBIVF_ERR_INVALID, "stored ids %d..%d fall outside the %lld base rows", ix->min_id, ix->max_id,
                         (long long)ix->dx.nbase);
     }
+    return GBIVF_OK;
+}
+
+// Coarse stage: coaidx/coadis (nq x w) for device queries d_q with norms qn.
+// The flags word w_flags holds [0] the device error flag, [1] the number of
+// centroids re-checked by the mixed form.
+int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, int w, unsigned flags, int32_t* coaidx,
+                 float* coadis, cudaStream_t st) {
+    const DevIndex& dx = ix->dx;
+    if (dx.C == 1) {
+        CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
+        return GBIVF_OK;
+    }
+    if (!(flags & GBIVF_MIXED_COARSE)) {
+        int bq = coarse_batch(nq, dx.C);
+        CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
+        float* cd = ix->w_cdist.as<float>();
+        for (int q0 = 0; q0 < nq; q0 += bq) {
+            int nb = std::min(bq, nq - q0);
+            CK(launch_coarse_dist(dx, d_q + (int64_t)q0 * dx.d, qn + q0, nb, cd, st));
+            CK(launch_coarse_select(cd, nb, dx.C, w, coaidx + (int64_t)q0 * w, coadis + (int64_t)q0 * w, st));
+        }
+        return GBIVF_OK;
+    }
+    if (!ix->coa_tiles.p) {
+        CK(ix->coa_tiles.ensure(coarse_mma_tile_bytes(dx.C, true)));
+        CK(launch_bf16_split_tiles(dx.coa, dx.C, ix->coa_tiles.as<uint8_t>(), st));
+        std::vector<float> len(dx.C);
+        std::vector<float> cn(dx.C);
+        CK(cudaMemcpyAsync(cn.data(), dx.coa_norm, sizeof(float) * dx.C, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int c = 0; c < dx.C; c++) len[c] = std::sqrt(cn[c]) * 1.0000002f;
+        CK(ix->coa_len.ensure(sizeof(float) * dx.C));
+        CK(cudaMemcpyAsync(ix->coa_len.p, len.data(), sizeof(float) * dx.C, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    int bq = coarse_batch(nq, dx.C);
+    if (bq >= MMA_QUERY_TILE) bq = bq / MMA_QUERY_TILE * MMA_QUERY_TILE;
+    CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
+    CK(ix->w_qtiles.ensure(coarse_mma_tile_bytes(bq, false)));
+    CK(ix->w_flags.ensure(2 * sizeof(int)));
+    CK(cudaMemsetAsync(ix->w_flags.p, 0, 2 * sizeof(int), st));
+    int* fl = ix->w_flags.as<int>();
+    for (int q0 = 0; q0 < nq; q0 += bq) {
+        int nb = std::min(bq, nq - q0);
+        const float* qb = d_q + (int64_t)q0 * dx.d;
+        CK(launch_bf16_tiles(qb, nb, MMA_QUERY_TILE, ix->w_qtiles.as<uint8_t>(), st));
+        CK(launch_coarse_mma(ix->w_qtiles.as<uint8_t>(), ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0,
+                             dx.coa_norm, ix->w_cdist.as<float>(), fl, st));
+        CK(launch_coarse_recheck(ix->w_cdist.as<float>(), nb, dx.C, w, qb, qn + q0, dx.coa, dx.coa_norm,
+                                 ix->coa_len.as<float>(), coaidx + (int64_t)q0 * w, coadis + (int64_t)q0 * w, fl + 1,
+                                 st));
+    }
+    ix->mixed_pending = true;
+    return GBIVF_OK;
+}
+
+// after a synchronised search: report a device-side timeout of the mixed coarse stage
+int check_device_flags(gbivf_index* ix) {
+    if (!ix->mixed_pending) return GBIVF_OK;
+    ix->mixed_pending = false;
+    int h[2] = {0, 0};
+    CK(cudaMemcpy(h, ix->w_flags.p, sizeof(h), cudaMemcpyDeviceToHost));
+    ix->last_ncand = h[1];
+    if (h[0]) return fail(GBIVF_ERR_TIMEOUT, "tensor-core coarse stage: a bounded wait ran out");
     return GBIVF_OK;
 }
 
@@ -318,17 +390,9 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     }
     ix->ev_valid = false;
     CK(launch_norm_d(d_q, nq, dx.d, qn, st));
-    if (dx.C == 1) {
-        CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
-    } else {
-        int bq = coarse_batch(nq, dx.C);
-        CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
-        float* cd = ix->w_cdist.as<float>();
-        for (int q0 = 0; q0 < nq; q0 += bq) {
-            int nb = std::min(bq, nq - q0);
-            CK(launch_coarse_dist(dx, d_q + (int64_t)q0 * dx.d, qn + q0, nb, cd, st));
-            CK(launch_coarse_select(cd, nb, dx.C, w, coaidx + (int64_t)q0 * w, coadis + (int64_t)q0 * w, st));
-        }
+    {
+        int rc = coarse_stage(ix, d_q, qn, nq, w, flags, coaidx, coadis, st);
+        if (rc) return rc;
     }
     ScanArgs a;
     a.nq = nq;
@@ -469,7 +533,7 @@ int gbivf_ivfpq_search(gbivf_index* ix, const float* queries, int nq, int k, int
     CK(cudaMemcpyAsync(ids, ix->w_ids.p, sizeof(int32_t) * ob, cudaMemcpyDeviceToHost, ix->stream));
     CK(cudaMemcpyAsync(dis, ix->w_dis.p, sizeof(float) * ob, cudaMemcpyDeviceToHost, ix->stream));
     CK(cudaStreamSynchronize(ix->stream));
-    return GBIVF_OK;
+    return check_device_flags(ix);
 }
 
 int gbivf_last_stage_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms) {
@@ -485,9 +549,14 @@ int gbivf_last_stage_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms) {
     return GBIVF_OK;
 }
 
-int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, int32_t* coaidx, float* coadis) {
+int gbivf_coarse_assign_flags(gbivf_index* ix, const float* queries, int nq, int w, unsigned flags, int32_t* coaidx,
+                              float* coadis, int64_t* ncand) {
     if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
     if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
+    if (flags & ~(GBIVF_MIXED_COARSE | GBIVF_PROFILE)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
+    if (ncand) *ncand = 0;
     if (nq <= 0) return nq == 0 ? GBIVF_OK : fail(GBIVF_ERR_INVALID, "nq=%d", nq);
     if (!queries || !coaidx || !coadis) return fail(GBIVF_ERR_INVALID, "NULL host buffer");
     std::lock_guard<std::mutex> lk(ix->mu);
@@ -500,19 +569,20 @@ int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, in
     CK(ix->w_coadis.ensure(sizeof(float) * (size_t)nq * w));
     CK(cudaMemcpyAsync(ix->w_q.p, queries, qb, cudaMemcpyHostToDevice, ix->stream));
     CK(launch_norm_d(ix->w_q.as<float>(), nq, dx.d, ix->w_qn.as<double>(), ix->stream));
-    int bq = coarse_batch(nq, dx.C);
-    CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
-    for (int q0 = 0; q0 < nq; q0 += bq) {
-        int nb = std::min(bq, nq - q0);
-        CK(launch_coarse_dist(dx, ix->w_q.as<float>() + (int64_t)q0 * dx.d, ix->w_qn.as<double>() + q0, nb,
-                              ix->w_cdist.as<float>(), ix->stream));
-        CK(launch_coarse_select(ix->w_cdist.as<float>(), nb, dx.C, w, ix->w_coaidx.as<int32_t>() + (int64_t)q0 * w,
-                                ix->w_coadis.as<float>() + (int64_t)q0 * w, ix->stream));
-    }
+    int rc = coarse_stage(ix, ix->w_q.as<float>(), ix->w_qn.as<double>(), nq, w, flags, ix->w_coaidx.as<int32_t>(),
+                          ix->w_coadis.as<float>(), ix->stream);
+    if (rc) return rc;
     CK(cudaMemcpyAsync(coaidx, ix->w_coaidx.p, sizeof(int32_t) * (size_t)nq * w, cudaMemcpyDeviceToHost, ix->stream));
     CK(cudaMemcpyAsync(coadis, ix->w_coadis.p, sizeof(float) * (size_t)nq * w, cudaMemcpyDeviceToHost, ix->stream));
     CK(cudaStreamSynchronize(ix->stream));
-    return GBIVF_OK;
+    ix->last_ncand = 0;
+    rc = check_device_flags(ix);
+    if (ncand) *ncand = ix->last_ncand;
+    return rc;
+}
+
+int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, int32_t* coaidx, float* coadis) {
+    return gbivf_coarse_assign_flags(ix, queries, nq, w, 0u, coaidx, coadis, nullptr);
 }
 
 int gbivf_core_gpu(gbivf_index* ix, const float* residual, int nres, const int32_t* rid_to_ivf,

@@ -71,6 +71,17 @@ bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
 
+// mixed-precision coarse stage (d = 128): BF16 tiles, tcgen05 GEMM, exact re-check
+cudaError_t launch_bf16_tiles(const float* x, int n, int rows_per_tile, uint8_t* out, cudaStream_t st);
+cudaError_t launch_bf16_split_tiles(const float* x, int n, uint8_t* out, cudaStream_t st);
+size_t coarse_mma_tile_bytes(int n, bool centroids);
+cudaError_t launch_coarse_mma(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C, const double* qnorm,
+                              const float* cnorm, float* out, int* err, cudaStream_t st);
+cudaError_t launch_coarse_recheck(const float* approx, int nq, int C, int w, const float* q, const double* qnorm,
+                                  const float* coa, const float* cnorm, const float* clen, int32_t* coaidx,
+                                  float* coadis, int* ncand, cudaStream_t st);
+constexpr int MMA_QUERY_TILE = 128;
+
 // largest k / kl / w the scan kernel supports
 constexpr int MAX_K = 2048;
 constexpr int MAX_W = 4096;

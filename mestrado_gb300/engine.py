@@ -81,7 +81,7 @@ class GpuIndex:
         return d.value, c.value, m.value, ks.value, n.value
 
     # -- searches ---------------------------------------------------------
-    def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None):
+    def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False):
         """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
         pass preallocated (ids, dis) host arrays (e.g. pinned memory)."""
         q = _c(queries, np.float32)
@@ -94,14 +94,16 @@ class GpuIndex:
             assert ids.shape == (nq, k) and ids.dtype == np.int32 and ids.flags.c_contiguous
             assert dis.shape == (nq, k) and dis.dtype == np.float32 and dis.flags.c_contiguous
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
+        flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
         return ids, dis
 
     def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      stream_ptr=0, profile=False):
+                      stream_ptr=0, profile=False, mixed_coarse=False):
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
+        flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
@@ -112,13 +114,18 @@ class GpuIndex:
         check(self.lib.gbivf_last_stage_ms(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def coarse_assign(self, queries, w):
+    def coarse_assign(self, queries, w, mixed=False, stats=False):
+        """knn_full over the coarse centroids: (coaidx, coadis) nq x w. With
+        mixed=True the tensor-core form runs (same results); stats=True also
+        returns the number of centroids it re-checked exactly."""
         q = _c(queries, np.float32)
         nq = q.shape[0]
         idx = np.empty((nq, w), np.int32)
         dis = np.empty((nq, w), np.float32)
-        check(self.lib.gbivf_coarse_assign(self.h, _p(q), nq, w, _p(idx), _p(dis)))
-        return idx, dis
+        nc = C.c_int64(0)
+        flags = _lib.GBIVF_MIXED_COARSE if mixed else 0
+        check(self.lib.gbivf_coarse_assign_flags(self.h, _p(q), nq, w, flags, _p(idx), _p(dis), C.byref(nc)))
+        return (idx, dis, nc.value) if stats else (idx, dis)
 
     def core_gpu(self, residual, rid_to_ivf, qid_to_starting_outid, nout, k, w):
         r = _c(residual, np.float32)
