@@ -100,6 +100,49 @@ int gbivf_ivfpq_search(gbivf_index *ix, const float *queries, int nq, int k, int
 int gbivf_ivfpq_search_device(gbivf_index *ix, const float *d_queries, int nq, int k, int kl,
                               int w, unsigned flags, int32_t *d_ids, float *d_dis, void *stream);
 
+/* Uneven batch (many queries with their own nprobe and k in one launch
+ * sequence, as the batched workload needs): query q probes w_per_q[q] lists
+ * (1..coarsek) and returns k_per_q[q] results; results are packed, query q's
+ * at the exclusive prefix sum of k_per_q (ids/dis hold sum(k_per_q)
+ * entries), ascending, -1 / +inf padded. No re-rank. Host buffers.
+ * No counterpart in the reference, whose calls share one k and w. */
+int gbivf_search_batched(gbivf_index *ix, const float *queries, int nq, const int32_t *w_per_q,
+                         const int32_t *k_per_q, unsigned flags, int32_t *ids, float *dis);
+
+/* Same with device buffers: d_w / d_k per query (values are clamped to
+ * 1..max_w / 1..max_k), d_out_off the output offset of each query; max_w and
+ * max_k bound them. Enqueued on `stream`; returns after launching. */
+int gbivf_search_batched_device(gbivf_index *ix, const float *d_queries, int nq, const int32_t *d_w,
+                                const int32_t *d_k, const int64_t *d_out_off, int max_w, int max_k,
+                                unsigned flags, int32_t *d_ids, float *d_dis, void *stream);
+
+/* A search captured as a CUDA graph, replayed with one launch.
+ * gbivf_graph_capture runs the described device-buffer search once on
+ * `stream` (sizing the index's workspace), then captures the same launch
+ * sequence; gbivf_graph_launch replays it on any stream with whatever the
+ * buffers hold at that time. Arguments are those of
+ * gbivf_ivfpq_search_device, plus optional d_w / d_k / d_out_off (all three,
+ * k and w as maxima) for an uneven batch as gbivf_search_batched_device
+ * takes them. Replays share the index's workspace: do not overlap them with
+ * other searches on the same index. */
+typedef struct gbivf_graph gbivf_graph;
+int gbivf_graph_capture(gbivf_index *ix, const float *d_queries, int nq, int k, int kl, int w,
+                        unsigned flags, int32_t *d_ids, float *d_dis, const int32_t *d_w,
+                        const int32_t *d_k, const int64_t *d_out_off, void *stream, gbivf_graph **out);
+int gbivf_graph_launch(gbivf_graph *g, void *stream);
+int gbivf_graph_destroy(gbivf_graph *g);
+
+/* Autotuner: times the scan kernels that can serve this index and search
+ * shape (persistent register-codebook kernel with 512 or 1024 threads, or the
+ * general kernel) on a calibration batch of device queries, keeps the fastest
+ * for later searches on this index and reports it in *choice (512, 1024, or
+ * 0 for the general kernel); times_ms (3 entries, may be NULL) receives each
+ * variant's scan time, -1 where it does not apply. When the environment
+ * variable GBIVF_TUNE_CACHE names a file, choices are read from and appended
+ * to it, keyed by index shape, list-size histogram, GPU and search shape. */
+int gbivf_index_autotune(gbivf_index *ix, const float *d_queries, int nq, int k, int kl, int w,
+                         unsigned flags, int *choice, float *times_ms);
+
 /* Stage times (milliseconds, CUDA events on the launching stream) of the
  * last search made with GBIVF_PROFILE: coarse assignment (query norms,
  * distances, k-min) and the fused scan (tables, ADC, top-k, re-rank).

@@ -24,6 +24,8 @@ EXPORTS = [
     "gbivf_index_set_base", "gbivf_index_destroy", "gbivf_index_dims", "gbivf_ivfpq_search",
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
     "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc", "gbivf_coarse_assign_flags",
+    "gbivf_search_batched", "gbivf_search_batched_device", "gbivf_graph_capture", "gbivf_graph_launch",
+    "gbivf_graph_destroy", "gbivf_index_autotune",
 ]
 
 
@@ -61,6 +63,12 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
     lib.gbivf_coarse_assign_flags.argtypes = [vp, vp, i32, i32, u32, vp, vp, vp]
+    lib.gbivf_search_batched.argtypes = [vp, vp, i32, vp, vp, u32, vp, vp]
+    lib.gbivf_search_batched_device.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, u32, vp, vp, vp]
+    lib.gbivf_graph_capture.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
+    lib.gbivf_graph_launch.argtypes = [vp, vp]
+    lib.gbivf_graph_destroy.argtypes = [vp]
+    lib.gbivf_index_autotune.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp]
     for name in EXPORTS:
         if name != "gbivf_last_error":
             getattr(lib, name).restype = i32

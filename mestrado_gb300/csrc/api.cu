@@ -372,8 +372,10 @@ int check_device_flags(gbivf_index* ix) {
 }
 
 // queries already on the device; everything enqueued on st
+// (uneven batches: d_w / d_k / d_off per query, w and k their maxima; NULL = uniform)
 int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl, int w, unsigned flags,
-                       int32_t* d_ids, float* d_dis, cudaStream_t st) {
+                       int32_t* d_ids, float* d_dis, cudaStream_t st, const int32_t* d_w = nullptr,
+                       const int32_t* d_k = nullptr, const int64_t* d_off = nullptr) {
     if (nq == 0) return GBIVF_OK;
     const DevIndex& dx = ix->dx;
     CK(ix->w_qn.ensure(sizeof(double) * nq));
@@ -405,6 +407,9 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.probes = coaidx;
     a.out_ids = d_ids;
     a.out_dis = d_dis;
+    a.w_per_q = d_w;
+    a.k_per_q = d_k;
+    a.out_off = d_off;
     if (prof) CK(cudaEventRecord(ix->ev[1], st));
     {
         int rs = run_scan(ix, a, st);
@@ -547,6 +552,257 @@ int gbivf_last_stage_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms) {
     if (coarse_ms) *coarse_ms = a;
     if (scan_ms) *scan_ms = b;
     return GBIVF_OK;
+}
+
+}  // extern "C"
+
+struct gbivf_graph {
+    gbivf_index* ix = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// the scan kernel choices the autotuner compares
+struct ScanVariant {
+    bool persistent;
+    int threads;
+};
+constexpr ScanVariant kVariants[3] = {{true, 512}, {true, 1024}, {false, 0}};
+
+std::string tune_key(gbivf_index* ix, int k, int w, unsigned flags) {
+    // index shape, a coarse histogram of list sizes, the GPU, and the search shape
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, ix->device) != cudaSuccess) p.name[0] = 0;
+    int64_t n = 0, mx = 0;
+    for (int32_t v : ix->h_len) {
+        n += v;
+        mx = std::max<int64_t>(mx, v);
+    }
+    int hist[8] = {0};
+    const double mean = ix->h_len.empty() ? 1.0 : std::max(1.0, (double)n / ix->h_len.size());
+    for (int32_t v : ix->h_len) {
+        int b = 0;
+        double r = v / mean;
+        while (b < 7 && r > 0.25 * (1 << b)) b++;
+        hist[b]++;
+    }
+    char buf[512];
+    snprintf(buf, sizeof buf, "d%d_C%d_m%d_n%lld_max%lld_h%d.%d.%d.%d.%d.%d.%d.%d_k%d_w%d_f%x_%s", ix->dx.d, ix->dx.C,
+             ix->dx.m, (long long)n, (long long)mx, hist[0], hist[1], hist[2], hist[3], hist[4], hist[5], hist[6],
+             hist[7], k, w, flags & ~GBIVF_PROFILE, p.name);
+    for (char* c = buf; *c; c++)
+        if (*c == ' ' || *c == '\n') *c = '_';
+    return buf;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbivf_graph_capture(gbivf_index* ix, const float* d_queries, int nq, int k, int kl, int w, unsigned flags,
+                        int32_t* d_ids, float* d_dis, const int32_t* d_w, const int32_t* d_k, const int64_t* d_out_off,
+                        void* stream, gbivf_graph** out) {
+    if (!out) return fail(GBIVF_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    const bool uneven = d_w || d_k || d_out_off;
+    if (uneven && !(d_w && d_k && d_out_off)) return fail(GBIVF_ERR_INVALID, "d_w, d_k and d_out_off go together");
+    if (uneven && (flags & GBIVF_RERANK)) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
+    flags &= ~GBIVF_PROFILE;
+    int rc = check_search(ix, nq, k, uneven ? k : kl, w, flags);
+    if (rc) return rc;
+    if (nq <= 0 || !d_queries || !d_ids || !d_dis) return fail(GBIVF_ERR_INVALID, "empty or NULL search");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    // one run sizes the workspace and prepares every lazily built buffer
+    rc = search_device_impl(ix, d_queries, nq, k, uneven ? k : kl, w, flags, d_ids, d_dis, st, d_w, d_k, d_out_off);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(st));
+    ix->mixed_pending = false;
+    auto* gr = new gbivf_graph();
+    gr->ix = ix;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        delete gr;
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    }
+    rc = search_device_impl(ix, d_queries, nq, k, uneven ? k : kl, w, flags, d_ids, d_dis, st, d_w, d_k, d_out_off);
+    e = cudaStreamEndCapture(st, &gr->graph);
+    ix->mixed_pending = false;
+    if (rc || e != cudaSuccess) {
+        if (gr->graph) cudaGraphDestroy(gr->graph);
+        delete gr;
+        return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&gr->exec, gr->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(gr->graph);
+        delete gr;
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    *out = gr;
+    return GBIVF_OK;
+}
+
+int gbivf_graph_launch(gbivf_graph* gr, void* stream) {
+    if (!gr || !gr->exec) return fail(GBIVF_ERR_INVALID, "graph is NULL");
+    DeviceGuard g(gr->ix->device);
+    CK(cudaGraphLaunch(gr->exec, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_graph_destroy(gbivf_graph* gr) {
+    if (!gr) return GBIVF_OK;
+    DeviceGuard g(gr->ix->device);
+    if (gr->exec) cudaGraphExecDestroy(gr->exec);
+    if (gr->graph) cudaGraphDestroy(gr->graph);
+    delete gr;
+    return GBIVF_OK;
+}
+
+int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k, int kl, int w, unsigned flags,
+                         int* choice, float* times_ms) {
+    int rc = check_search(ix, nq, k, kl, w, flags);
+    if (rc) return rc;
+    if (nq <= 0 || !d_queries) return fail(GBIVF_ERR_INVALID, "empty calibration batch");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const std::string key = tune_key(ix, k, w, flags);
+    const char* cache = getenv("GBIVF_TUNE_CACHE");
+    if (cache) {  // "key threads" lines; threads 0 = the general kernel
+        if (FILE* f = fopen(cache, "r")) {
+            char kbuf[600];
+            int th = -1;
+            while (fscanf(f, "%599s %d", kbuf, &th) == 2) {
+                if (key == kbuf) {
+                    ix->use_persistent = th != 0;
+                    ix->scan_threads = th == 1024 ? 1024 : 512;
+                    if (choice) *choice = th;
+                    if (times_ms) times_ms[0] = times_ms[1] = times_ms[2] = -1.0f;
+                    fclose(f);
+                    return GBIVF_OK;
+                }
+            }
+            fclose(f);
+        }
+    }
+    const size_t ob = (size_t)nq * k;
+    CK(ix->w_ids.ensure(sizeof(int32_t) * ob));
+    CK(ix->w_dis.ensure(sizeof(float) * ob));
+    CK(ix->w_queue.ensure(sizeof(int)));
+    const bool save_p = ix->use_persistent;
+    const int save_t = ix->scan_threads;
+    float best = 1e30f;
+    int best_i = -1;
+    for (int i = 0; i < 3; i++) {
+        ix->use_persistent = kVariants[i].persistent;
+        ix->scan_threads = kVariants[i].persistent ? kVariants[i].threads : save_t;
+        float t = -1.0f;
+        ScanArgs probe;
+        probe.nq = nq;
+        probe.w = w;
+        probe.k = k;
+        probe.kl = kl;
+        probe.flags = flags & GBIVF_RERANK ? SCAN_RERANK : 0;
+        probe.queue = ix->w_queue.as<int>();
+        const bool applies = !kVariants[i].persistent || scan_persistent_supported(ix->dx, probe);
+        if (applies) {
+            float sum = 0.0f;
+            for (int rep = 0; rep < 3 && rc == GBIVF_OK; rep++) {
+                rc = search_device_impl(ix, d_queries, nq, k, kl, w, flags | GBIVF_PROFILE, ix->w_ids.as<int32_t>(),
+                                        ix->w_dis.as<float>(), ix->stream);
+                if (rc) break;
+                CK(cudaStreamSynchronize(ix->stream));
+                float cm = 0, sm = 0;
+                CK(cudaEventElapsedTime(&cm, ix->ev[0], ix->ev[1]));
+                CK(cudaEventElapsedTime(&sm, ix->ev[1], ix->ev[2]));
+                if (rep > 0) sum += sm;
+            }
+            if (rc) break;
+            t = sum / 2.0f;
+            if (t < best) {
+                best = t;
+                best_i = i;
+            }
+        }
+        if (times_ms) times_ms[i] = t;
+    }
+    ix->mixed_pending = false;
+    if (rc || best_i < 0) {
+        ix->use_persistent = save_p;
+        ix->scan_threads = save_t;
+        return rc ? rc : fail(GBIVF_ERR_INVALID, "no scan kernel applies");
+    }
+    ix->use_persistent = kVariants[best_i].persistent;
+    ix->scan_threads = kVariants[best_i].persistent ? kVariants[best_i].threads : save_t;
+    const int th = kVariants[best_i].persistent ? kVariants[best_i].threads : 0;
+    if (choice) *choice = th;
+    if (cache)
+        if (FILE* f = fopen(cache, "a")) {
+            fprintf(f, "%s %d\n", key.c_str(), th);
+            fclose(f);
+        }
+    return GBIVF_OK;
+}
+
+int gbivf_search_batched_device(gbivf_index* ix, const float* d_queries, int nq, const int32_t* d_w,
+                                const int32_t* d_k, const int64_t* d_out_off, int max_w, int max_k, unsigned flags,
+                                int32_t* d_ids, float* d_dis, void* stream) {
+    if (flags & GBIVF_RERANK) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
+    int rc = check_search(ix, nq, max_k, max_k, max_w, flags);
+    if (rc) return rc;
+    if (nq > 0 && (!d_queries || !d_w || !d_k || !d_out_off || !d_ids || !d_dis))
+        return fail(GBIVF_ERR_INVALID, "NULL device buffer");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    return search_device_impl(ix, d_queries, nq, max_k, max_k, max_w, flags, d_ids, d_dis, (cudaStream_t)stream, d_w,
+                              d_k, d_out_off);
+}
+
+int gbivf_search_batched(gbivf_index* ix, const float* queries, int nq, const int32_t* w_per_q,
+                         const int32_t* k_per_q, unsigned flags, int32_t* ids, float* dis) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    if (nq == 0) return GBIVF_OK;
+    if (!queries || !w_per_q || !k_per_q || !ids || !dis) return fail(GBIVF_ERR_INVALID, "NULL host buffer");
+    if (flags & GBIVF_RERANK) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
+    int max_w = 0, max_k = 0;
+    std::vector<int64_t> off(nq);
+    int64_t total = 0;
+    for (int q = 0; q < nq; q++) {
+        if (w_per_q[q] < 1 || w_per_q[q] > ix->dx.C)
+            return fail(GBIVF_ERR_INVALID, "w_per_q[%d]=%d outside 1..%d", q, w_per_q[q], ix->dx.C);
+        if (k_per_q[q] < 1) return fail(GBIVF_ERR_INVALID, "k_per_q[%d]=%d", q, k_per_q[q]);
+        max_w = std::max(max_w, w_per_q[q]);
+        max_k = std::max(max_k, k_per_q[q]);
+        off[q] = total;
+        total += k_per_q[q];
+    }
+    int rc = check_search(ix, nq, max_k, max_k, max_w, flags);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const size_t qb = sizeof(float) * (size_t)nq * ix->dx.d;
+    CK(ix->w_q.ensure(qb));
+    CK(ix->w_ids.ensure(sizeof(int32_t) * (size_t)total));
+    CK(ix->w_dis.ensure(sizeof(float) * (size_t)total));
+    CK(ix->w_res.ensure(sizeof(int32_t) * (2 * (size_t)nq + 2) + sizeof(int64_t) * (size_t)nq));
+    int32_t* dw = ix->w_res.as<int32_t>();
+    int32_t* dk = dw + nq;
+    int64_t* doff = reinterpret_cast<int64_t*>(dk + nq + (nq & 1));
+    CK(cudaMemcpyAsync(ix->w_q.p, queries, qb, cudaMemcpyHostToDevice, ix->stream));
+    CK(cudaMemcpyAsync(dw, w_per_q, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, ix->stream));
+    CK(cudaMemcpyAsync(dk, k_per_q, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, ix->stream));
+    CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * nq, cudaMemcpyHostToDevice, ix->stream));
+    rc = search_device_impl(ix, ix->w_q.as<float>(), nq, max_k, max_k, max_w, flags, ix->w_ids.as<int32_t>(),
+                            ix->w_dis.as<float>(), ix->stream, dw, dk, doff);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ids, ix->w_ids.p, sizeof(int32_t) * (size_t)total, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaMemcpyAsync(dis, ix->w_dis.p, sizeof(float) * (size_t)total, cudaMemcpyDeviceToHost, ix->stream));
+    CK(cudaStreamSynchronize(ix->stream));
+    return check_device_flags(ix);
 }
 
 int gbivf_coarse_assign_flags(gbivf_index* ix, const float* queries, int nq, int w, unsigned flags, int32_t* coaidx,

@@ -197,20 +197,21 @@ __global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a
 
     if (!src_res)
         for (int i = tid; i < d; i += SC_NT) xq[i] = a.queries[(int64_t)q * d + i];
+    const int wq = query_w(a, q);  // probes used by this query (w is the row stride)
     if (tid == 0) {
         uint32_t acc = 0;
-        for (int j = 0; j < w; j++) {
+        for (int j = 0; j < wq; j++) {
             int l = a.probes[(int64_t)q * w + j];
             plist[j] = l;
             prefix[j] = acc;
             acc += (l >= 0) ? (uint32_t)ix.list_len[l] : 0u;
         }
-        prefix[w] = acc;
+        prefix[wq] = acc;
     }
-    const int kk = rerank ? a.kl : a.k;
+    const int kk = rerank ? a.kl : query_k(a, q);
     topk_init(s, kk);
 
-    for (int j = 0; j < w; j++) {
+    for (int j = 0; j < wq; j++) {
         const int l = plist[j];
         if (l < 0) continue;
         // residual (bsxfunMINUS) or given residual row
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(SC_NT) ivf_scan_kernel(DevIndex ix, ScanArgs a
         __syncthreads();
     }
     topk_finish(s);
-    scan_epilogue(ix, a, s, q, prefix, plist, cand, xq);
+    scan_epilogue(ix, a, s, q, prefix, plist, cand, xq, wq);
 }
 
 template <int M>

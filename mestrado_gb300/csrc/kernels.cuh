@@ -48,7 +48,24 @@ struct ScanArgs {
     int32_t* cand_id = nullptr;
     int32_t* cand_cnt = nullptr;
     int cand_stride = 0;
+    // uneven batches: per-query probe count (<= w, the probes row stride) and
+    // result count (<= k), results of query q at out_off[q]; NULL = uniform
+    const int32_t* w_per_q = nullptr;
+    const int32_t* k_per_q = nullptr;
+    const int64_t* out_off = nullptr;
 };
+
+// per-query shape of a (possibly uneven) batch
+// (values outside 1..w / 1..k are clamped, so a bad entry cannot overrun buffers)
+__device__ __forceinline__ int query_w(const ScanArgs& a, int q) {
+    return a.w_per_q ? min(max(a.w_per_q[q], 1), a.w) : a.w;
+}
+__device__ __forceinline__ int query_k(const ScanArgs& a, int q) {
+    return a.k_per_q ? min(max(a.k_per_q[q], 1), a.k) : a.k;
+}
+__device__ __forceinline__ int64_t query_out(const ScanArgs& a, int q) {
+    return a.out_off ? a.out_off[q] : (int64_t)q * a.k;
+}
 
 // query norms: double accumulation of float squares (nn.c:137-142)
 cudaError_t launch_norm_d(const float* x, int64_t n, int d, double* out, cudaStream_t st);

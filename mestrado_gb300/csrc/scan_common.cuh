@@ -99,8 +99,10 @@ __device__ __forceinline__ int32_t pos_to_id(const DevIndex& ix, const uint32_t*
 // exact re-rank of the kl candidates (ivf_search.cpp:113-134) and write k.
 // xq holds the query (re-rank needs it). Uniform control flow.
 __device__ inline void scan_epilogue(const DevIndex& ix, const ScanArgs& a, TopKSmem& s, int q, const uint32_t* prefix,
-                              const int* plist, int* cand, const float* xq) {
-    const int tid = threadIdx.x, nt = blockDim.x, w = a.w;
+                              const int* plist, int* cand, const float* xq, int w) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int kq = query_k(a, q);
+    const int64_t oq = query_out(a, q);
     const int nb = *s.nbest;
     const float inf = __int_as_float(0x7f800000);
     if (!(a.flags & SCAN_RERANK)) {
@@ -111,16 +113,16 @@ __device__ inline void scan_epilogue(const DevIndex& ix, const ScanArgs& a, TopK
                 a.out_dis[o + c] = key_dist(s.best[c]);
             }
         } else {
-            for (int c = tid; c < a.k; c += nt) {
-                a.out_ids[(int64_t)q * a.k + c] = c < nb ? pos_to_id(ix, prefix, plist, w, key_payload(s.best[c])) : -1;
-                a.out_dis[(int64_t)q * a.k + c] = c < nb ? key_dist(s.best[c]) : inf;
+            for (int c = tid; c < kq; c += nt) {
+                a.out_ids[oq + c] = c < nb ? pos_to_id(ix, prefix, plist, w, key_payload(s.best[c])) : -1;
+                a.out_dis[oq + c] = c < nb ? key_dist(s.best[c]) : inf;
             }
         }
         return;
     }
     for (int c = tid; c < nb; c += nt) cand[c] = pos_to_id(ix, prefix, plist, w, key_payload(s.best[c]));
     __syncthreads();
-    const int kr = min(a.k, nb);
+    const int kr = min(kq, nb);
     if (kr > 0) {
         topk_init(s, kr);
         const double qn = a.qnorm[q];
@@ -152,9 +154,9 @@ __device__ inline void scan_epilogue(const DevIndex& ix, const ScanArgs& a, TopK
         }
         topk_finish(s);
     }
-    for (int c = tid; c < a.k; c += nt) {
-        a.out_ids[(int64_t)q * a.k + c] = c < kr ? cand[key_payload(s.best[c])] : -1;
-        a.out_dis[(int64_t)q * a.k + c] = c < kr ? key_dist(s.best[c]) : inf;
+    for (int c = tid; c < kq; c += nt) {
+        a.out_ids[oq + c] = c < kr ? cand[key_payload(s.best[c])] : -1;
+        a.out_dis[oq + c] = c < kr ? key_dist(s.best[c]) : inf;
     }
 }
 

@@ -73,9 +73,8 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     int* qslot = reinterpret_cast<int*>(smem + L.off_misc);  // [1] = next query
     TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, SP_BCAP, smem + L.off_work};
 
-    const int tid = threadIdx.x, lane = tid & 31, w = a.w;
+    const int tid = threadIdx.x, lane = tid & 31, w = a.w;  // w: the probes row stride
     const bool src_res = a.flags & SCAN_SRC_RESIDUAL;
-    const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
 
     // this thread's slice of the codebook: sub-quantizer my_s, centroids
     // my_c0 .. my_c0+E-1 (consecutive, so the table row is one vector store)
@@ -107,15 +106,18 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
         if (q >= a.nq) break;
         __syncthreads();
         if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
+        // this query's probe count and result count (uneven batches)
+        const int wq = query_w(a, q);
+        const int kq = (a.flags & SCAN_RERANK) ? a.kl : query_k(a, q);
         if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
         // probe lists and their prefix sums, one warp
         if (tid < 32) {
             uint32_t carry = 0;
-            for (int j0 = 0; j0 < w; j0 += 32) {
+            for (int j0 = 0; j0 < wq; j0 += 32) {
                 const int j = j0 + lane;
                 int l = -1;
                 uint32_t len = 0;
-                if (j < w) {
+                if (j < wq) {
                     l = __ldg(a.probes + (int64_t)q * w + j);
                     len = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
                     plist[j] = l;
@@ -126,19 +128,19 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= o) incl += v;
                 }
-                if (j < w) prefix[j] = carry + incl - len;
+                if (j < wq) prefix[j] = carry + incl - len;
                 carry += __shfl_sync(0xffffffffu, incl, 31);
             }
-            if (lane == 0) prefix[w] = carry;
+            if (lane == 0) prefix[wq] = carry;
         }
-        topk_init(s, kk);
+        topk_init(s, kq);
 
-        for (int j = 0; j < w; j++) {
+        for (int j = 0; j < wq; j++) {
             const int jr = j % SP_RCH;
             if (jr == 0) {
                 // residuals of probes j .. j+SP_RCH-1 (bsxfunMINUS) and their
                 // sub-norms (the a-operand norm of compute_cross_distances)
-                const int nr = min(SP_RCH, w - j);
+                const int nr = min(SP_RCH, wq - j);
                 for (int e = tid; e < nr * D; e += NT) {
                     const int p = e / D, x = e % D, l = plist[j + p];
                     float v = 0.0f;
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             // count is read between it and the next one, before new appends
             __syncthreads();
             const int nb = *s.nbuf;
-            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kk && nb >= kk) || nb >= SP_SOFT;
+            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kq && nb >= kq) || nb >= SP_SOFT;
             __syncthreads();
             if (flush_now) topk_flush(s, nb);
             // ADC scan of the list, software-pipelined one chunk ahead; the
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const int64_t o = (int64_t)q * a.cand_stride + c;
             if (c < nbest) {
                 a.cand_key[o] = best[c];
-                a.cand_id[o] = pos_to_id(ix, prefix, plist, w, key_payload(best[c]));
+                a.cand_id[o] = pos_to_id(ix, prefix, plist, wq, key_payload(best[c]));
             } else {
                 a.cand_key[o] = KEY_MAX;
                 a.cand_id[o] = -1;
@@ -325,9 +327,11 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
                 a.out_dis[o + c] = key_dist(keys[c]);
             }
         } else {
-            for (int c = tid; c < a.k; c += FIN_NT) {
-                a.out_ids[(int64_t)q * a.k + c] = c < n ? ids[c] : -1;
-                a.out_dis[(int64_t)q * a.k + c] = c < n ? key_dist(keys[c]) : inf;
+            const int kq = query_k(a, q);
+            const int64_t o = query_out(a, q);
+            for (int c = tid; c < kq; c += FIN_NT) {
+                a.out_ids[o + c] = c < n ? ids[c] : -1;
+                a.out_dis[o + c] = c < n ? key_dist(keys[c]) : inf;
             }
         }
         return;
@@ -353,10 +357,12 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     }
     __syncthreads();
     bitonic_sort_smem(keys, n2);
-    const int kr = min(a.k, n);
-    for (int c = tid; c < a.k; c += FIN_NT) {
-        a.out_ids[(int64_t)q * a.k + c] = c < kr ? ids[key_payload(keys[c])] : -1;
-        a.out_dis[(int64_t)q * a.k + c] = c < kr ? key_dist(keys[c]) : inf;
+    const int kq = query_k(a, q);
+    const int64_t o = query_out(a, q);
+    const int kr = min(kq, n);
+    for (int c = tid; c < kq; c += FIN_NT) {
+        a.out_ids[o + c] = c < kr ? ids[key_payload(keys[c])] : -1;
+        a.out_dis[o + c] = c < kr ? key_dist(keys[c]) : inf;
     }
 }
 

@@ -108,6 +108,40 @@ class GpuIndex:
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
 
+    def search_batched(self, queries, w_per_q, k_per_q, mixed_coarse=False):
+        """Uneven batch: per-query nprobe and k. Returns (ids, dis, offsets):
+        query q's results are ids[offsets[q]:offsets[q+1]]."""
+        q = _c(queries, np.float32)
+        wq = _c(w_per_q, np.int32)
+        kq = _c(k_per_q, np.int32)
+        off = np.zeros(len(kq) + 1, np.int64)
+        np.cumsum(kq, out=off[1:])
+        ids = np.empty(int(off[-1]), np.int32)
+        dis = np.empty(int(off[-1]), np.float32)
+        flags = _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
+        check(self.lib.gbivf_search_batched(self.h, _p(q), q.shape[0], _p(wq), _p(kq), flags, _p(ids), _p(dis)))
+        return ids, dis, off
+
+    def capture_graph(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
+                      mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0):
+        """Capture a device-buffer search as a CUDA graph (see gbivf_graph_capture)."""
+        flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
+        g = C.c_void_p()
+        check(self.lib.gbivf_graph_capture(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
+                                           flags, C.c_void_p(d_ids_ptr), C.c_void_p(d_dis_ptr), C.c_void_p(d_w_ptr),
+                                           C.c_void_p(d_k_ptr), C.c_void_p(d_off_ptr), C.c_void_p(stream_ptr),
+                                           C.byref(g)))
+        return SearchGraph(self.lib, g)
+
+    def autotune(self, d_queries_ptr, nq, k, w, kl=None, rerank=False, mixed_coarse=False):
+        """Pick the fastest scan kernel for this index; returns (choice, times_ms)."""
+        flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
+        ch = C.c_int()
+        t = (C.c_float * 3)()
+        check(self.lib.gbivf_index_autotune(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
+                                            flags, C.byref(ch), t))
+        return ch.value, list(t)
+
     def last_stage_ms(self):
         """(coarse_ms, scan_ms) of the last search made with profile=True."""
         a, b = C.c_float(), C.c_float()
@@ -135,6 +169,28 @@ class GpuIndex:
         dists = np.full(nout, np.nan, np.float32)
         check(self.lib.gbivf_core_gpu(self.h, _p(r), r.shape[0], _p(rid), _p(qs), _p(idxs), _p(dists), k, w))
         return idxs, dists
+
+
+class SearchGraph:
+    """A captured search; launch() replays it on a stream."""
+
+    def __init__(self, lib, h):
+        self.lib = lib
+        self.h = h
+
+    def launch(self, stream_ptr=0):
+        check(self.lib.gbivf_graph_launch(self.h, C.c_void_p(stream_ptr)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbivf_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class GpuPQ(GpuIndex):
