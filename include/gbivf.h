@@ -203,6 +203,39 @@ int gbivf_pq_create(gbivf_index **out, int device, int d, int nsq, int ks, const
 int gbivf_pq_search(gbivf_index *ix, const float *queries, int nq, int k, float *dis,
                     int32_t *ids);
 
+/* ---- index building on the GPU (device buffers; return when done) ----
+ * The reference trains and encodes on one CPU thread with yael's k-means and
+ * exact 1-NN (sequential/ivf_pq/ivf_new.cpp:4-33, ivf_assign.cpp:3-52,
+ * pq-utils/pq_new.cpp:6-59, pq-utils/pq_assign.cpp:12-53); these replace
+ * those steps for large base sets. Assignment to d = 128 centroids runs on
+ * the tensor cores; centroid sums accumulate in FP64. */
+
+/* n x d byte-valued vectors of a Gaussian mixture: component c (uniform, or
+ * drawn through d_cdf, the cumulative weights of ncomp components), value
+ * clip(round(means[c] + sigma * N(0,1)), 0, 255). Counter-based: rows
+ * row0 .. row0+n-1 of stream `stream_id` are the same whatever the chunking. */
+int gbivf_generate_mixture(float *d_out, int64_t n, int d, const float *d_means, int ncomp,
+                           const double *d_cdf, float sigma, uint64_t seed, uint64_t stream_id,
+                           int64_t row0, void *stream);
+
+/* Lloyd k-means, niter iterations (d = 128, or 8, 16, 32), k x d centroids. */
+int gbivf_kmeans(const float *d_x, int64_t n, int d, int k, int niter, uint64_t seed,
+                 float *d_centroids, void *stream);
+
+/* Nearest of k centroids for each of n rows (d = 128, or 8, 16, 32). */
+int gbivf_assign(const float *d_x, int64_t n, int d, const float *d_centroids, int k,
+                 int32_t *d_assign, void *stream);
+
+/* Sub-quantizers: m k-means of 256 centroids on the sub-vectors of the
+ * residuals d_r (n x d); d_pq receives m x 256 x (d/m). */
+int gbivf_pq_train(const float *d_r, int64_t n, int d, int m, int niter, uint64_t seed, float *d_pq,
+                   void *stream);
+
+/* PQ codes (n x m bytes) of rows d_x, of their residuals to d_coa[d_coarse[i]]
+ * when d_coarse is not NULL. */
+int gbivf_pq_encode(const float *d_x, int64_t n, int d, const int32_t *d_coarse, const float *d_coa,
+                    int m, const float *d_pq, uint8_t *d_codes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,8 @@ EXPORTS = [
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
     "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc", "gbivf_coarse_assign_flags",
     "gbivf_search_batched", "gbivf_search_batched_device", "gbivf_graph_capture", "gbivf_graph_launch",
-    "gbivf_graph_destroy", "gbivf_index_autotune",
+    "gbivf_graph_destroy", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
+    "gbivf_pq_train", "gbivf_pq_encode",
 ]
 
 
@@ -69,6 +70,12 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_graph_launch.argtypes = [vp, vp]
     lib.gbivf_graph_destroy.argtypes = [vp]
     lib.gbivf_index_autotune.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp]
+    u64 = C.c_uint64
+    lib.gbivf_generate_mixture.argtypes = [vp, i64, i32, vp, i32, vp, C.c_float, u64, u64, i64, vp]
+    lib.gbivf_kmeans.argtypes = [vp, i64, i32, i32, i32, u64, vp, vp]
+    lib.gbivf_assign.argtypes = [vp, i64, i32, vp, i32, vp, vp]
+    lib.gbivf_pq_train.argtypes = [vp, i64, i32, i32, i32, u64, vp, vp]
+    lib.gbivf_pq_encode.argtypes = [vp, i64, i32, vp, vp, i32, vp, vp, vp]
     for name in EXPORTS:
         if name != "gbivf_last_error":
             getattr(lib, name).restype = i32

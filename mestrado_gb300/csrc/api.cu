@@ -995,3 +995,60 @@ extern "C" int gbivf_coarse_assign_noalloc(gbivf_index* ix, const float* d_queri
     CK(launch_coarse_select(dist, nq, dx.C, w, d_coaidx, d_coadis, st));
     return GBIVF_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Index building on the GPU (build_gpu.cu). Synchronous; device buffers.
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int gbivf_generate_mixture(float* d_out, int64_t n, int d, const float* d_means, int ncomp, const double* d_cdf,
+                           float sigma, uint64_t seed, uint64_t stream_id, int64_t row0, void* stream) {
+    if (!d_out || !d_means || n < 0 || d <= 0 || d % 2 || ncomp <= 0)
+        return fail(GBIVF_ERR_INVALID, "bad mixture arguments");
+    CK(gen_mixture(d_out, n, d, d_means, ncomp, d_cdf, sigma, seed, stream_id, row0, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_kmeans(const float* d_x, int64_t n, int d, int k, int niter, uint64_t seed, float* d_centroids,
+                 void* stream) {
+    if (!d_x || !d_centroids || n <= 0 || k <= 0 || niter < 0) return fail(GBIVF_ERR_INVALID, "bad k-means arguments");
+    if (d != 128 && d != 8 && d != 16 && d != 32)
+        return fail(GBIVF_ERR_UNSUPPORTED, "k-means on the GPU takes d = 128 (tensor cores) or 8, 16, 32");
+    CK(kmeans_rows(d_x, n, d, d, k, niter, seed, d_centroids, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_assign(const float* d_x, int64_t n, int d, const float* d_centroids, int k, int32_t* d_assign,
+                 void* stream) {
+    if (!d_x || !d_centroids || !d_assign || n < 0 || k <= 0) return fail(GBIVF_ERR_INVALID, "bad assign arguments");
+    if (d != 128 && d != 8 && d != 16 && d != 32)
+        return fail(GBIVF_ERR_UNSUPPORTED, "assignment on the GPU takes d = 128 or 8, 16, 32");
+    if (n == 0) return GBIVF_OK;
+    cudaError_t e = assign_rows(d_x, n, d, d, d_centroids, k, d_assign, (cudaStream_t)stream);
+    if (e == cudaErrorLaunchTimeout) return fail(GBIVF_ERR_TIMEOUT, "tensor-core assignment: a bounded wait ran out");
+    CK(e);
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_pq_train(const float* d_r, int64_t n, int d, int m, int niter, uint64_t seed, float* d_pq, void* stream) {
+    if (!d_r || !d_pq || n <= 0 || m <= 0 || d % m) return fail(GBIVF_ERR_INVALID, "bad PQ training arguments");
+    const int ds = d / m;
+    if (ds != 8 && ds != 16 && ds != 32) return fail(GBIVF_ERR_UNSUPPORTED, "sub-vector length %d (8, 16, 32)", ds);
+    CK(pq_train_rows(d_r, n, d, m, niter, seed, d_pq, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_pq_encode(const float* d_x, int64_t n, int d, const int32_t* d_coarse, const float* d_coa, int m,
+                    const float* d_pq, uint8_t* d_codes, void* stream) {
+    if (!d_x || !d_pq || !d_codes || n < 0 || m <= 0 || d % m || (d_coarse && !d_coa))
+        return fail(GBIVF_ERR_INVALID, "bad PQ encode arguments");
+    const int ds = d / m;
+    if (ds != 8 && ds != 16 && ds != 32) return fail(GBIVF_ERR_UNSUPPORTED, "sub-vector length %d (8, 16, 32)", ds);
+    if (n == 0) return GBIVF_OK;
+    CK(pq_encode_rows(d_x, n, d, d_coarse, d_coa, m, d_pq, d_codes, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+}  // extern "C"

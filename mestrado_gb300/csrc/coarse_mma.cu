@@ -120,10 +120,13 @@ __global__ void bf16_split_tiles_kernel(const float* __restrict__ x, int n, int 
     *reinterpret_cast<uint4*>(base + B_HALF_BYTES) = *reinterpret_cast<const uint4*>(lo);
 }
 
+// out != NULL: approximate distances, nq x C row-major. amin != NULL instead:
+// per (row, centroid tile) the smallest (distance, centroid) key, nq x gridDim.x.
 __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restrict__ qtiles,
                                                          const uint8_t* __restrict__ ctiles, int nq, int C,
                                                          const double* __restrict__ qnorm,
                                                          const float* __restrict__ cnorm, float* __restrict__ out,
+                                                         unsigned long long* __restrict__ amin,
                                                          int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* sA = sm;
@@ -194,6 +197,7 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
     if (ok) {
         const int row = qt * MM_M + warp * 32 + lane;
         const float qn = row < nq ? (float)qnorm[row] : 0.0f;
+        u64 best = KEY_MAX;
 #pragma unroll 1
         for (int ch = 0; ch < MM_N / 32; ch++) {
             uint32_t r[32];
@@ -209,7 +213,12 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
                 : "r"(ta));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             const int c0 = ct * MM_N + ch * 32;
-            if (row < nq) {
+            if (amin) {
+                for (int j = 0; j < 32 && c0 + j < C; j++) {
+                    const u64 key = make_key(qn + cnorm[c0 + j] - 2.0f * __uint_as_float(r[j]), (uint32_t)(c0 + j));
+                    best = key < best ? key : best;
+                }
+            } else if (row < nq) {
                 float* o = out + (int64_t)row * C + c0;
                 if (c0 + 32 <= C && (C & 3) == 0) {
 #pragma unroll
@@ -226,6 +235,7 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
                 }
             }
         }
+        if (amin && row < nq) amin[(int64_t)row * gridDim.x + ct] = best;
     } else if (tid == 0) {
         atomicExch(err, 1);
     }
@@ -323,15 +333,18 @@ size_t coarse_mma_tile_bytes(int n, bool centroids) {
 }
 
 cudaError_t launch_coarse_mma(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C, const double* qnorm,
-                              const float* cnorm, float* out, int* err, cudaStream_t st) {
+                              const float* cnorm, float* out, int* err, cudaStream_t st,
+                              unsigned long long* amin) {
     if (nq <= 0) return cudaSuccess;
     const size_t sm = A_TILE_BYTES + B_TILE_BYTES + 64;
     cudaError_t e = cudaFuncSetAttribute(coarse_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     dim3 grid((C + MM_N - 1) / MM_N, (nq + MM_M - 1) / MM_M);
-    coarse_mma_kernel<<<grid, 128, sm, st>>>(qtiles, ctiles, nq, C, qnorm, cnorm, out, err);
+    coarse_mma_kernel<<<grid, 128, sm, st>>>(qtiles, ctiles, nq, C, qnorm, cnorm, amin ? nullptr : out, amin, err);
     return cudaGetLastError();
 }
+
+int coarse_mma_ctiles(int C) { return (C + MM_N - 1) / MM_N; }
 
 cudaError_t launch_coarse_recheck(const float* approx, int nq, int C, int w, const float* q, const double* qnorm,
                                   const float* coa, const float* cnorm, const float* clen, int32_t* coaidx,

@@ -92,12 +92,28 @@ int scan_persistent_stride(const ScanArgs& a);
 cudaError_t launch_bf16_tiles(const float* x, int n, int rows_per_tile, uint8_t* out, cudaStream_t st);
 cudaError_t launch_bf16_split_tiles(const float* x, int n, uint8_t* out, cudaStream_t st);
 size_t coarse_mma_tile_bytes(int n, bool centroids);
+// out: nq x C approximate distances; or, with amin, per (query, 128-centroid
+// tile) the smallest (distance, centroid) key, nq x coarse_mma_ctiles(C)
 cudaError_t launch_coarse_mma(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C, const double* qnorm,
-                              const float* cnorm, float* out, int* err, cudaStream_t st);
+                              const float* cnorm, float* out, int* err, cudaStream_t st,
+                              unsigned long long* amin = nullptr);
+int coarse_mma_ctiles(int C);
 cudaError_t launch_coarse_recheck(const float* approx, int nq, int C, int w, const float* q, const double* qnorm,
                                   const float* coa, const float* cnorm, const float* clen, int32_t* coaidx,
                                   float* coadis, int* ncand, cudaStream_t st);
 constexpr int MMA_QUERY_TILE = 128;
+
+// index building (build_gpu.cu); synchronous, allocate their own temporaries
+cudaError_t assign_rows(const float* x, int64_t n, int64_t ld, int d, const float* cent, int k, int32_t* assign,
+                        cudaStream_t st);
+cudaError_t kmeans_rows(const float* x, int64_t n, int64_t ld, int d, int k, int niter, uint64_t seed, float* cent,
+                        cudaStream_t st);
+cudaError_t gen_mixture(float* out, int64_t n, int d, const float* means, int ncomp, const double* cdf, float sigma,
+                        uint64_t seed, uint64_t stream_id, int64_t row0, cudaStream_t st);
+cudaError_t pq_train_rows(const float* r, int64_t n, int d, int m, int niter, uint64_t seed, float* pq,
+                          cudaStream_t st);
+cudaError_t pq_encode_rows(const float* x, int64_t n, int d, const int32_t* coarse, const float* coa, int m,
+                           const float* pq, uint8_t* codes, cudaStream_t st);
 
 // largest k / kl / w the scan kernel supports
 constexpr int MAX_K = 2048;

@@ -1,0 +1,133 @@
+"""Build large IVF-PQ indexes on the GPU, through the engine's C ABI.
+
+The reference trains and encodes on one CPU thread (ivfpq_new + ivfpq_assign,
+sequential/ivf_test.cpp:52-59); at 10M+ base vectors that is impractical, so
+this driver runs every step on the GPU:
+
+1. mixture data (gbivf_generate_mixture: counter-based, chunked);
+2. coarse k-means (gbivf_kmeans: tensor-core assignment, FP64 centroid sums);
+3. residuals of the training set, then m sub-quantizer k-means (gbivf_pq_train);
+4. base vectors: nearest coarse centroid (gbivf_assign), PQ codes of the
+   residuals (gbivf_pq_encode);
+5. lists bucketed by coarse centroid with ids ascending (stable sort on the
+   host, as the reference's ivec_sort_index orders them).
+
+Device buffers are torch tensors (memory only); all compute is the engine's.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .ivfdata import IVFPQData
+from .synth import Mixture
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def zipf_cdf(ncomp: int, s: float) -> np.ndarray:
+    w = 1.0 / np.arange(1, ncomp + 1, dtype=np.float64) ** s
+    c = np.cumsum(w)
+    return c / c[-1]
+
+
+class GpuMixture:
+    """A Mixture whose vectors are generated on the GPU in chunks."""
+
+    def __init__(self, mx: Mixture, device="cuda"):
+        import torch
+
+        self.mx = mx
+        self.lib = _lib.load()
+        self.means = torch.from_numpy(mx.means()).to(device)
+        self.cdf = torch.from_numpy(zipf_cdf(mx.ncomp, mx.zipf)).to(device) if mx.zipf else None
+        self.device = device
+
+    def generate(self, n: int, stream_id: int, row0: int = 0, out=None, chunk: int = 1 << 24):
+        import torch
+
+        d = self.mx.d
+        if out is None:
+            out = torch.empty((n, d), dtype=torch.float32, device=self.device)
+        s = torch.cuda.current_stream().cuda_stream
+        for r in range(0, n, chunk):
+            nb = min(chunk, n - r)
+            check(self.lib.gbivf_generate_mixture(
+                C.c_void_p(out.data_ptr() + r * d * 4), nb, d, _ptr(self.means), self.mx.ncomp,
+                _ptr(self.cdf) if self.cdf is not None else C.c_void_p(0), float(self.mx.sigma),
+                self.mx.seed, stream_id, row0 + r, C.c_void_p(s)))
+        return out
+
+
+def train_quantizers(train, coarsek: int, m: int, niter: int = 10, seed: int = 0):
+    """(coarse centroids, pq centroids) as device tensors."""
+    import torch
+
+    lib = _lib.load()
+    n, d = train.shape
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    coa = torch.empty((coarsek, d), dtype=torch.float32, device=train.device)
+    check(lib.gbivf_kmeans(_ptr(train), n, d, coarsek, niter, seed, _ptr(coa), s))
+    assign = torch.empty(n, dtype=torch.int32, device=train.device)
+    check(lib.gbivf_assign(_ptr(train), n, d, _ptr(coa), coarsek, _ptr(assign), s))
+    res = train - coa[assign.long()]
+    pq = torch.empty((m, 256, d // m), dtype=torch.float32, device=train.device)
+    check(lib.gbivf_pq_train(_ptr(res), n, d, m, niter, seed + 1, _ptr(pq), s))
+    return coa, pq
+
+
+def encode_base(base, coa, pq, chunk: int = 1 << 24):
+    """(coarse assignment, codes) of the base set, device tensors."""
+    import torch
+
+    lib = _lib.load()
+    n, d = base.shape
+    m = pq.shape[0]
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assign = torch.empty(n, dtype=torch.int32, device=base.device)
+    codes = torch.empty((n, m), dtype=torch.uint8, device=base.device)
+    for r in range(0, n, chunk):
+        nb = min(chunk, n - r)
+        xb = base[r:r + nb]
+        ab = assign[r:r + nb]
+        check(lib.gbivf_assign(_ptr(xb), nb, d, _ptr(coa), coa.shape[0], _ptr(ab), s))
+        check(lib.gbivf_pq_encode(_ptr(xb), nb, d, _ptr(ab), _ptr(coa), m, _ptr(pq), _ptr(codes[r:r + nb]), s))
+    return assign, codes
+
+
+def bucket(assign: np.ndarray, codes: np.ndarray, coarsek: int):
+    order = np.argsort(assign, kind="stable")
+    counts = np.bincount(assign, minlength=coarsek)
+    off = np.zeros(coarsek + 1, np.int64)
+    np.cumsum(counts, out=off[1:])
+    return off, order.astype(np.int32), np.ascontiguousarray(codes[order])
+
+
+def build_index_gpu(base, train, coarsek: int, m: int, niter: int = 10, seed: int = 0) -> IVFPQData:
+    coa, pq = train_quantizers(train, coarsek, m, niter, seed)
+    assign, codes = encode_base(base, coa, pq)
+    off, ids, codes_h = bucket(assign.cpu().numpy(), codes.cpu().numpy(), coarsek)
+    out = IVFPQData(coa=coa.cpu().numpy(), pq=pq.cpu().numpy(), list_off=off, ids=ids, codes=codes_h)
+    out.validate()
+    return out
+
+
+def exact_topk(base, queries, k: int, batch: int = 256):
+    """Brute-force top-k by squared L2 on the GPU. For byte-valued vectors (d <=
+    256) every product and partial sum is an integer below 2^24, so FP32 gives
+    the exact distances (the same as FP64). Evaluation only."""
+    import torch
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    bn = (base * base).sum(1)
+    out = np.empty((queries.shape[0], k), np.int64)
+    for s in range(0, queries.shape[0], batch):
+        q = queries[s:s + batch]
+        dist = (q * q).sum(1, keepdim=True) + bn[None, :] - 2.0 * (q @ base.T)
+        out[s:s + len(q)] = torch.topk(dist, k, dim=1, largest=False).indices.cpu().numpy()
+    return out
