@@ -47,6 +47,18 @@ CONFIGS = {
                  w=4, k=100, kl=100, rerank=True, train_iters=10),
 }
 
+# Larger workloads, generated and indexed on the GPU (gbivf_generate_mixture,
+# gbivf_kmeans, gbivf_pq_encode): the precision form against the plain one.
+LARGE = {
+    # 10M base, 4,096-component mixture, 65,536 lists, m = 8, 10k queries, w = 32, k = 100
+    "cfg3": dict(d=128, ncomp=4096, seed=0, zipf=None, nbase=10_000_000, ntrain=1_000_000, nq=10_000,
+                 C=65536, m=8, w=32, k=100, uneven=False, train_iters=8, recall_q=1000),
+    # 100M base, Zipf(1.1) cluster sizes over 262,144 lists, m = 16, 32,768 queries with
+    # nprobe log-uniform in [1, 256] and k from {1, 10, 100, 1000}
+    "cfg4": dict(d=128, ncomp=262144, seed=0, zipf=1.1, nbase=100_000_000, ntrain=2_621_440, nq=32768,
+                 C=262144, m=16, w=256, k=1000, uneven=True, train_iters=6, recall_q=256),
+}
+
 CACHE = os.environ.get("MESTRADO_GB300_CACHE", "/tmp/mestrado_gb300_cache")
 L2_FLUSH_BYTES = 256 << 20
 
@@ -358,13 +370,137 @@ def run_gpu(args, c, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def run_large(args, c, name, local_rank):
+    """Larger workloads: data and index built on the GPU; the plain FP32 form and
+    the precision form (tensor-core coarse stage) timed as CUDA-graph replays."""
+    import torch
+
+    from mestrado_gb300.engine import GpuIndex
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu, exact_topk
+    from mestrado_gb300.synth import Mixture
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    t0 = time.time()
+    gm = GpuMixture(Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"], zipf=c["zipf"]))
+    base = gm.generate(c["nbase"], stream_id=1)
+    train = gm.generate(c["ntrain"], stream_id=2)
+    queries = gm.generate(c["nq"], stream_id=3)
+    torch.cuda.synchronize()
+    t_gen = time.time() - t0
+    t0 = time.time()
+    ix = build_index_gpu(base, train, c["C"], c["m"], niter=c["train_iters"], seed=c["seed"])
+    t_build = time.time() - t0
+    del train
+    sizes = ix.list_sizes()
+    log(f"{name}: generated in {t_gen:.1f}s, index built in {t_build:.1f}s; lists {sizes.min()}..{sizes.max()}")
+    gi = GpuIndex(ix, device=local_rank)
+    nq = c["nq"]
+    rng = np.random.default_rng(c["seed"] + 17)
+    if c["uneven"]:
+        wq = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(c["w"] + 1), nq))), 1, c["w"]).astype(np.int32)
+        kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
+    else:
+        wq = np.full(nq, c["w"], np.int32)
+        kq = np.full(nq, c["k"], np.int32)
+    off = np.concatenate([[0], np.cumsum(kq)]).astype(np.int64)
+    max_w, max_k = int(wq.max()), int(kq.max())
+    d_w = torch.from_numpy(wq).to(dev)
+    d_k = torch.from_numpy(kq).to(dev)
+    d_off = torch.from_numpy(off[:-1].copy()).to(dev)
+    d_ids = torch.empty(int(off[-1]), dtype=torch.int32, device=dev)
+    d_dis = torch.empty(int(off[-1]), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    # candidate bytes of the ADC scan: sum over queries of their probed lists' codes
+    coa_idx, _ = gi.coarse_assign(queries.cpu().numpy(), max_w)
+    scan_bytes = int(sum(sizes[coa_idx[i, :wq[i]]].sum() for i in range(nq))) * c["m"]
+    sample = min(nq, c["recall_q"])
+    gt = exact_topk(base, queries[:sample], max_k, batch=16 if c["nbase"] > 20_000_000 else 64)
+
+    forms = {}
+    for form, mixed in (("plain", False), ("mixed", True)):
+        graph = gi.capture_graph(queries.data_ptr(), nq, max_k, max_w, d_ids.data_ptr(), d_dis.data_ptr(),
+                                 mixed_coarse=mixed, d_w_ptr=d_w.data_ptr(), d_k_ptr=d_k.data_ptr(),
+                                 d_off_ptr=d_off.data_ptr(), stream_ptr=sp)
+        for i in range(args.warmup):
+            graph.launch(sp)
+        stream.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        clocks = ClockSampler(local_rank)
+        clocks.start()
+        total = 0.0
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xff)
+                ev0.record(stream)
+            graph.launch(sp)
+            with torch.cuda.stream(stream):
+                ev1.record(stream)
+            ev1.synchronize()
+            total += ev0.elapsed_time(ev1)
+        clk = clocks.stop()
+        graph.close()
+        ids = d_ids.cpu().numpy()
+        # stage split from one profiled (non-graph) run
+        gi.lib.gbivf_search_batched_device(gi.h, C_ptr(queries), nq, C_ptr(d_w), C_ptr(d_k), C_ptr(d_off),
+                                           max_w, max_k, 0x100 | (0x4 if mixed else 0), C_ptr(d_ids),
+                                           C_ptr(d_dis), sp_ptr(sp))
+        cm, sm = gi.last_stage_ms()
+        rec = [len(set(ids[off[i]:off[i] + kq[i]].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i]
+               for i in range(sample)]
+        forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps,
+                           coarse_ms=cm, scan_ms=sm, recall=float(np.mean(rec)), clocks=clk, ids=ids)
+    same = bool(np.array_equal(forms["plain"]["ids"], forms["mixed"]["ids"]))
+    peak, peak_kind = measured_peak_hbm()
+    mx = forms["mixed"]
+    achieved = scan_bytes / (mx["scan_ms"] / 1000.0) / 1e9
+    wl = (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture"
+          f"{', Zipf ' + str(c['zipf']) if c['zipf'] else ''}), C={c['C']:,} lists, m={c['m']}x256, "
+          f"{nq:,} queries/step, " + (f"nprobe log-uniform 1..{c['w']}, k in {{1,10,100,1000}}" if c["uneven"]
+                                        else f"w={c['w']}, k={c['k']}"))
+    line = {
+        "metric": "QPS", "value": mx["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (coarse on bf16 tensor cores + fp32 re-check)", "data": "synthetic",
+        "config": {"workload": wl, "form": "mixed (tensor-core coarse stage), CUDA-graph replay",
+                   "plain_qps": forms["plain"]["qps"], "speedup_vs_plain": mx["qps"] / forms["plain"]["qps"],
+                   "identical_ids_plain_vs_mixed": same, f"recall_sample_queries": sample,
+                   "recall_mixed": mx["recall"], "recall_plain": forms["plain"]["recall"],
+                   "stage_ms_mixed": {"coarse": mx["coarse_ms"], "scan": mx["scan_ms"]},
+                   "stage_ms_plain": {"coarse": forms["plain"]["coarse_ms"], "scan": forms["plain"]["scan_ms"]},
+                   "index_build_s": t_build, "generate_s": t_gen, "l2": "flushed between steps (256 MB write)"},
+        "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": scan_bytes,
+                     "traffic": None},
+        "cpu_baseline": None,
+        "clocks": mx["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    gi.close()
+
+
+def C_ptr(t):
+    import ctypes
+
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def sp_ptr(s):
+    import ctypes
+
+    return ctypes.c_void_p(s)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbivf", choices=["gbivf", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS) + sorted(LARGE))
     ap.add_argument("--ref-sample", type=int, default=10_000, help="queries per CPU step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
@@ -372,10 +508,18 @@ def main():
     if args.warmup < 3:
         log(f"--warmup {args.warmup} raised to 3 (at least 3 untimed warm-up steps)")
         args.warmup = 3
-    c = CONFIGS[args.config]
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.config in LARGE:
+        if args.impl == "reference" or world > 1:
+            if rank == 0:
+                print(json.dumps({"impl": args.impl, "unavailable": "the large configurations run the GPU engine "
+                                  "alone, on one GPU (the CPU oracle over 10M-100M vectors takes hours)"}))
+            return
+        run_large(args, LARGE[args.config], args.config, local_rank)
+        return
+    c = CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, c, rank, world)
     else:

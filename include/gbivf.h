@@ -42,6 +42,9 @@ extern "C" {
 #define GBIVF_TABLE_DIRECT 0x2u /* tables as sum (r-c)^2 (parallel2) instead of the expansion */
 #define GBIVF_MIXED_COARSE 0x4u /* coarse stage as a BF16 tensor-core GEMM + exact FP32 re-check (d = 128);
                                    the probed lists are identical to the plain path's */
+#define GBIVF_COARSE_FULL 0x8u  /* large C (>= 16384, w <= 1024): keep the full C-wide distance block and
+                                   select from it, instead of the default sample-bound candidate filter;
+                                   the results are the same either way */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -176,10 +179,18 @@ int gbivf_coarse_assign_noalloc(gbivf_index *ix, const float *d_queries, int nq,
                                 int32_t *d_coaidx, float *d_coadis, void *stream);
 
 /* gbivf_coarse_assign with search flags (GBIVF_MIXED_COARSE selects the
- * tensor-core form). `ncand`, when not NULL, receives the number of
- * centroids the mixed form re-checked exactly (0 for the plain form). */
+ * tensor-core form, GBIVF_COARSE_FULL the full-block selection). `ncand`,
+ * when not NULL, receives the number of centroids re-checked exactly after
+ * the first pass (0 for the plain form over the full block). */
 int gbivf_coarse_assign_flags(gbivf_index *ix, const float *queries, int nq, int w, unsigned flags,
                               int32_t *coaidx, float *coadis, int64_t *ncand);
+
+/* Work counters of the last gbivf_coarse_assign_flags call: centroids whose
+ * distance was computed exactly after the first pass (the candidates of the
+ * mixed form or of the large-C filter) and queries for which the large-C
+ * filter's sample bound proved too low, so that all C centroids were taken
+ * exactly. Either may be NULL. No counterpart in the reference. */
+int gbivf_last_coarse_stats(gbivf_index *ix, int64_t *rechecked, int64_t *fallback_queries);
 
 /* core_gpu(PQ, residual, ivf, ivf_size, rid_to_ivf, qid_to_starting_outid,
  * idxs, dists, k, w) (parallel2/ivf_pq/mycuda.cu:119-188): residual is

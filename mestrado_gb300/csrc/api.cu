@@ -108,8 +108,9 @@ struct gbivf_index {
     std::vector<int32_t> h_len;  // list sizes (host copy)
     int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
     int num_sms = 0;
-    bool mixed_pending = false;       // a mixed coarse stage ran since the last flag check
-    int64_t last_ncand = 0;
+    bool mixed_pending = false;       // a coarse stage with device flags ran since the last flag check
+    int64_t last_ncand = 0;           // centroids re-checked exactly by the last checked coarse stage
+    int64_t last_fallbacks = 0;       // queries of it that took all C centroids exactly
     bool use_persistent = true;       // register-codebook scan where the shape allows
     int scan_threads = 512;           // block size of the persistent scan (512 or 1024)
     std::vector<void*> owned;    // index allocations
@@ -120,6 +121,8 @@ struct gbivf_index {
     DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue, w_ckey, w_cid, w_ccnt;
     // mixed-precision coarse stage: centroid BF16 tiles, centroid lengths, query tiles, flags
     DBuf coa_tiles, coa_len, w_qtiles, w_flags;
+    // filtered coarse stage (large C): per-query bounds, counters, candidate slots
+    DBuf w_thr, w_fcnt, w_cand;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
     bool ev_valid = false;
 };
@@ -142,7 +145,8 @@ void free_index(gbivf_index* ix) {
     ix->owned.clear();
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
-                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->w_qtiles, &ix->w_flags})
+                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->w_qtiles, &ix->w_flags,
+                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -292,7 +296,7 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (k <= 0 || k > MAX_K) return fail(k <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "k=%d (1..%d)", k, MAX_K);
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
-    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE))
+    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL))
         return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
     if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
@@ -306,9 +310,71 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     return GBIVF_OK;
 }
 
+// BF16 centroid tiles and centroid lengths of the mixed form, built once
+int prepare_mixed(gbivf_index* ix, cudaStream_t st) {
+    if (ix->coa_tiles.p) return GBIVF_OK;
+    const DevIndex& dx = ix->dx;
+    CK(ix->coa_tiles.ensure(coarse_mma_tile_bytes(dx.C, true)));
+    CK(launch_bf16_split_tiles(dx.coa, dx.C, ix->coa_tiles.as<uint8_t>(), st));
+    std::vector<float> len(dx.C);
+    std::vector<float> cn(dx.C);
+    CK(cudaMemcpyAsync(cn.data(), dx.coa_norm, sizeof(float) * dx.C, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int c = 0; c < dx.C; c++) len[c] = std::sqrt(cn[c]) * 1.0000002f;
+    CK(ix->coa_len.ensure(sizeof(float) * dx.C));
+    CK(cudaMemcpyAsync(ix->coa_len.p, len.data(), sizeof(float) * dx.C, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return GBIVF_OK;
+}
+
+// Filtered coarse stage (coarse_filter.cu) for large C, plain or mixed form.
+int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, int nq, int w, bool mixed, int S,
+                          int r, int cap, int32_t* coaidx, float* coadis, int* fl, cudaStream_t st) {
+    const DevIndex& dx = ix->dx;
+    // queries per block: the sample block (bq x S floats) within 256 Mi floats
+    int64_t bq = std::min<int64_t>(nq, std::max<int64_t>(MMA_QUERY_TILE, (256ll << 20) / S));
+    bq = std::min<int64_t>(bq, 65535ll * 64);
+    if (bq >= MMA_QUERY_TILE) bq = bq / MMA_QUERY_TILE * MMA_QUERY_TILE;
+    CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * S));
+    CK(ix->w_thr.ensure(sizeof(float) * (size_t)bq));
+    CK(ix->w_fcnt.ensure(2 * sizeof(int) * (size_t)bq));
+    CK(ix->w_cand.ensure(sizeof(int32_t) * (size_t)bq * cap));
+    if (mixed) CK(ix->w_qtiles.ensure(coarse_mma_tile_bytes((int)bq, false)));
+    float* cd = ix->w_cdist.as<float>();
+    float* thr = ix->w_thr.as<float>();
+    int* cnt = ix->w_fcnt.as<int>();
+    CoarseFilter f;
+    f.thr = thr;
+    f.cnt = mixed ? cnt : nullptr;
+    f.ncand = cnt + bq;
+    f.cand = ix->w_cand.as<int32_t>();
+    f.cap = cap;
+    f.clen = mixed ? ix->coa_len.as<float>() : nullptr;
+    DevIndex sx = dx;  // the sample: the first S centroids
+    sx.C = S;
+    for (int64_t q0 = 0; q0 < nq; q0 += bq) {
+        const int nb = (int)std::min<int64_t>(bq, nq - q0);
+        const float* qb = d_q + q0 * dx.d;
+        CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int) * (size_t)bq, st));
+        if (mixed) {
+            uint8_t* qt = ix->w_qtiles.as<uint8_t>();
+            CK(launch_bf16_tiles(qb, nb, MMA_QUERY_TILE, qt, st));
+            CK(launch_coarse_mma(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, cd, fl, st));
+            CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, dx.coa_norm, ix->coa_len.as<float>(), thr, st));
+            CK(launch_coarse_mma_filter(qt, ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0, dx.coa_norm, f, fl, st));
+        } else {
+            CK(launch_coarse_dist(sx, qb, qn + q0, nb, cd, st));
+            CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, nullptr, nullptr, thr, st));
+            CK(launch_coarse_dist_filter(dx, qb, qn + q0, nb, f, st));
+        }
+        CK(launch_coarse_cand_select(dx, qb, qn + q0, nb, w, f, coaidx + q0 * w, coadis + q0 * w, fl + 1, st));
+    }
+    return GBIVF_OK;
+}
+
 // Coarse stage: coaidx/coadis (nq x w) for device queries d_q with norms qn.
 // The flags word w_flags holds [0] the device error flag, [1] the number of
-// centroids re-checked by the mixed form.
+// centroids re-checked exactly, [2] the queries that took all C centroids.
 int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, int w, unsigned flags, int32_t* coaidx,
                  float* coadis, cudaStream_t st) {
     const DevIndex& dx = ix->dx;
@@ -316,7 +382,22 @@ int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, in
         CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
         return GBIVF_OK;
     }
-    if (!(flags & GBIVF_MIXED_COARSE)) {
+    const bool mixed = flags & GBIVF_MIXED_COARSE;
+    int S = 0, r = 0, cap = 0;
+    if (coarse_filter_shape(dx.C, w, dx.d, &S, &r, &cap) && !(flags & GBIVF_COARSE_FULL)) {
+        if (mixed) {
+            int rc = prepare_mixed(ix, st);
+            if (rc) return rc;
+        }
+        CK(ix->w_flags.ensure(4 * sizeof(int)));
+        CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
+        int rc = coarse_stage_filtered(ix, d_q, qn, nq, w, mixed, S, r, cap, coaidx, coadis, ix->w_flags.as<int>(),
+                                       st);
+        if (rc) return rc;
+        ix->mixed_pending = true;
+        return GBIVF_OK;
+    }
+    if (!mixed) {
         int bq = coarse_batch(nq, dx.C);
         CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
         float* cd = ix->w_cdist.as<float>();
@@ -327,24 +408,16 @@ int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, in
         }
         return GBIVF_OK;
     }
-    if (!ix->coa_tiles.p) {
-        CK(ix->coa_tiles.ensure(coarse_mma_tile_bytes(dx.C, true)));
-        CK(launch_bf16_split_tiles(dx.coa, dx.C, ix->coa_tiles.as<uint8_t>(), st));
-        std::vector<float> len(dx.C);
-        std::vector<float> cn(dx.C);
-        CK(cudaMemcpyAsync(cn.data(), dx.coa_norm, sizeof(float) * dx.C, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        for (int c = 0; c < dx.C; c++) len[c] = std::sqrt(cn[c]) * 1.0000002f;
-        CK(ix->coa_len.ensure(sizeof(float) * dx.C));
-        CK(cudaMemcpyAsync(ix->coa_len.p, len.data(), sizeof(float) * dx.C, cudaMemcpyHostToDevice, st));
-        CK(cudaStreamSynchronize(st));
+    {
+        int rc = prepare_mixed(ix, st);
+        if (rc) return rc;
     }
     int bq = coarse_batch(nq, dx.C);
     if (bq >= MMA_QUERY_TILE) bq = bq / MMA_QUERY_TILE * MMA_QUERY_TILE;
     CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
     CK(ix->w_qtiles.ensure(coarse_mma_tile_bytes(bq, false)));
-    CK(ix->w_flags.ensure(2 * sizeof(int)));
-    CK(cudaMemsetAsync(ix->w_flags.p, 0, 2 * sizeof(int), st));
+    CK(ix->w_flags.ensure(4 * sizeof(int)));
+    CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
     int* fl = ix->w_flags.as<int>();
     for (int q0 = 0; q0 < nq; q0 += bq) {
         int nb = std::min(bq, nq - q0);
@@ -364,9 +437,10 @@ int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, in
 int check_device_flags(gbivf_index* ix) {
     if (!ix->mixed_pending) return GBIVF_OK;
     ix->mixed_pending = false;
-    int h[2] = {0, 0};
+    int h[3] = {0, 0, 0};
     CK(cudaMemcpy(h, ix->w_flags.p, sizeof(h), cudaMemcpyDeviceToHost));
     ix->last_ncand = h[1];
+    ix->last_fallbacks = h[2];
     if (h[0]) return fail(GBIVF_ERR_TIMEOUT, "tensor-core coarse stage: a bounded wait ran out");
     return GBIVF_OK;
 }
@@ -809,7 +883,8 @@ int gbivf_coarse_assign_flags(gbivf_index* ix, const float* queries, int nq, int
                               float* coadis, int64_t* ncand) {
     if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
     if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
-    if (flags & ~(GBIVF_MIXED_COARSE | GBIVF_PROFILE)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if (flags & ~(GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL | GBIVF_PROFILE))
+        return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
     if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
     if (ncand) *ncand = 0;
@@ -832,9 +907,17 @@ int gbivf_coarse_assign_flags(gbivf_index* ix, const float* queries, int nq, int
     CK(cudaMemcpyAsync(coadis, ix->w_coadis.p, sizeof(float) * (size_t)nq * w, cudaMemcpyDeviceToHost, ix->stream));
     CK(cudaStreamSynchronize(ix->stream));
     ix->last_ncand = 0;
+    ix->last_fallbacks = 0;
     rc = check_device_flags(ix);
     if (ncand) *ncand = ix->last_ncand;
     return rc;
+}
+
+int gbivf_last_coarse_stats(gbivf_index* ix, int64_t* rechecked, int64_t* fallback_queries) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (rechecked) *rechecked = ix->last_ncand;
+    if (fallback_queries) *fallback_queries = ix->last_fallbacks;
+    return GBIVF_OK;
 }
 
 int gbivf_coarse_assign(gbivf_index* ix, const float* queries, int nq, int w, int32_t* coaidx, float* coadis) {

@@ -1,0 +1,191 @@
+// Filtered coarse stage for large coarse quantizers.
+//
+// knn_full over C centroids (sequential/ivf_pq/ivf_search.cpp:37-38) keeps the
+// w nearest of C per query. Writing the whole nq x C distance block and
+// selecting from it costs 8 bytes of HBM traffic per (query, centroid) and a
+// long latency-bound selection per query; at C = 262,144 that is most of a
+// search. For large C the stage runs as:
+//
+//   1. a sample: distances (exact for the plain form, approximate for the
+//      tensor-core form) to the first S ~ C/8 centroids;
+//   2. per query, T = the r-th smallest of the sample (upper bounds approx +
+//      eps in the mixed form), r about twice w * S / C, so that about 2w
+//      centroids of the whole set fall below T;
+//   3. the full distance pass (SIMT or tcgen05) appends every centroid that
+//      can fall below T (exact <= T; approx - eps <= T) to the query's
+//      candidate slots and, in the mixed form, counts the centroids that
+//      certainly do (approx + eps <= T);
+//   4. per query, if at least w centroids certainly fall below T, the true w
+//      nearest are among the candidates: their exact distances (the
+//      reference's FP32 arithmetic, nn.c:143-145 and 85-86) and the keyed
+//      top-w give the plain path's result bit for bit. Otherwise (too few
+//      below T, or more candidates than slots) the query takes all C
+//      centroids exactly -- slow, rare and still exact.
+//
+// The result never depends on the sample: T only decides how much work the
+// candidate set takes.
+#include <algorithm>
+#include <cmath>
+
+#include "block_topk.cuh"
+#include "kernels.cuh"
+
+namespace gbivf {
+
+constexpr int KT_NT = 128, KT_ITEMS = 8;  // sample selection
+constexpr int CC_NT = 128;                // candidate selection
+
+static int pow2_ge(int x) {
+    int p = 2;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+static size_t cand_select_smem(int w, int cap, int d) {
+    const int kcap = pow2_ge(std::max(w, 2));
+    const int bcap = std::max(std::max(cap, 2 * CC_NT), kcap);
+    return sizeof(u64) * (2 * (size_t)kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int) + sizeof(float) * d;
+}
+
+bool coarse_filter_shape(int C, int w, int d, int* S, int* r, int* cap) {
+    if (C < 16384 || w < 1 || w > 1024) return false;
+    int s = std::max(4096, (C / 8 + 127) / 128 * 128);
+    s = std::min(s, C);
+    const int rr = std::min(s, (int)std::ceil(2.0 * w * (double)s / (double)C) + 8);
+    const int cp = pow2_ge(std::max(1024, 8 * w));
+    if (cand_select_smem(w, cp, d) > 200 * 1024) return false;
+    *S = s;
+    *r = rr;
+    *cap = cp;
+    return true;
+}
+
+// thr[q] = r-th smallest of row q (plus mixed_eps when clen != NULL)
+__global__ void __launch_bounds__(KT_NT) coarse_sample_kth_kernel(const float* __restrict__ vals, int S, int r,
+                                                                  const double* __restrict__ qnorm,
+                                                                  const float* __restrict__ cnorm,
+                                                                  const float* __restrict__ clen, int kcap, int bcap,
+                                                                  float* __restrict__ thr) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* best = reinterpret_cast<u64*>(smem);
+    u64* tmp = best + kcap;
+    u64* buf = tmp + kcap;
+    u64* thresh = buf + bcap;
+    unsigned char* work = reinterpret_cast<unsigned char*>(thresh + 1);
+    int* cnt = reinterpret_cast<int*>(work + TOPK_WORK_BYTES);
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, work};
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const float* row = vals + (int64_t)q * S;
+    const float qn = (float)qnorm[q];
+    const float qlen = sqrtf(qn);
+    topk_init(s, r);
+    for (int i0 = 0; i0 < S; i0 += KT_NT * KT_ITEMS) {
+#pragma unroll
+        for (int it = 0; it < KT_ITEMS; it++) {
+            const int c = i0 + it * KT_NT + tid;
+            const bool valid = c < S;
+            float v = valid ? row[c] : 0.0f;
+            if (clen && valid) v = v + mixed_eps(qn, qlen, cnorm[c], clen[c]);
+            topk_offer(s, make_key(v, (uint32_t)c), valid);
+        }
+        topk_round_end(s, KT_NT * KT_ITEMS);
+    }
+    topk_finish(s);
+    if (tid == 0) thr[q] = key_dist(best[min(r, *s.nbest) - 1]);
+}
+
+cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, const double* qnorm,
+                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (r < 1 || r > S) return cudaErrorInvalidValue;
+    const int kcap = pow2_ge(std::max(r, 2));
+    const int bcap = pow2_ge(std::max(2 * KT_NT * KT_ITEMS, kcap));
+    const size_t sm = sizeof(u64) * (2 * (size_t)kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int);
+    if (sm > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(coarse_sample_kth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    coarse_sample_kth_kernel<<<nq, KT_NT, sm, st>>>(vals, S, r, qnorm, cnorm, clen, kcap, bcap, thr);
+    return cudaGetLastError();
+}
+
+// Per query: exact keyed top-w over its candidates, or over all C centroids
+// when the candidates cannot be trusted to hold the w nearest.
+__global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* __restrict__ X, int d,
+                                                                   const float* __restrict__ coa, int C,
+                                                                   const double* __restrict__ qnorm,
+                                                                   const float* __restrict__ cnorm, int w,
+                                                                   CoarseFilter f, int kcap, int bcap,
+                                                                   int32_t* __restrict__ coaidx,
+                                                                   float* __restrict__ coadis, int* __restrict__ stats) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* best = reinterpret_cast<u64*>(smem);
+    u64* tmp = best + kcap;
+    u64* buf = tmp + kcap;
+    u64* thresh = buf + bcap;
+    unsigned char* work = reinterpret_cast<unsigned char*>(thresh + 1);
+    int* cnt = reinterpret_cast<int*>(work + TOPK_WORK_BYTES);
+    float* xq = reinterpret_cast<float*>(cnt + 2);
+    TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, work};
+    const int q = blockIdx.x, tid = threadIdx.x;
+    for (int l = tid; l < d; l += CC_NT) xq[l] = X[(int64_t)q * d + l];
+    const double qn = qnorm[q];
+    const int n = f.ncand[q];
+    const int below = f.cnt ? f.cnt[q] : n;
+    const bool all = n > f.cap || below < w;
+    topk_init(s, w);  // (its barrier also publishes xq)
+    if (!all) {
+        // n <= cap <= bcap: every candidate fits the buffer, no flush until the end
+        const int32_t* cq = f.cand + (int64_t)q * f.cap;
+        for (int i0 = 0; i0 < n; i0 += CC_NT) {
+            const int i = i0 + tid;
+            u64 key = 0;
+            if (i < n) {
+                const int c = cq[i];
+                key = make_key(expansion_from(qn, cnorm[c], dot_seq(coa + (int64_t)c * d, xq, d)), (uint32_t)c);
+            }
+            topk_offer(s, key, i < n);
+        }
+    } else {
+        for (int i0 = 0; i0 < C; i0 += CC_NT) {
+            const int c = i0 + tid;
+            u64 key = 0;
+            if (c < C) key = make_key(expansion_from(qn, cnorm[c], dot_seq(coa + (int64_t)c * d, xq, d)), (uint32_t)c);
+            topk_offer(s, key, c < C);
+            topk_round_end(s, CC_NT);
+        }
+    }
+    topk_finish(s);
+    const int nb = *s.nbest;
+    for (int j = tid; j < w; j += CC_NT) {
+        coaidx[(int64_t)q * w + j] = j < nb ? (int32_t)key_payload(best[j]) : -1;
+        coadis[(int64_t)q * w + j] = j < nb ? key_dist(best[j]) : __int_as_float(0x7f800000);
+    }
+    if (tid == 0 && stats) {
+        atomicAdd(&stats[0], all ? C : n);
+        if (all) atomicAdd(&stats[1], 1);
+    }
+}
+
+cudaError_t launch_coarse_cand_select(const DevIndex& ix, const float* q, const double* qnorm, int nq, int w,
+                                      const CoarseFilter& f, int32_t* coaidx, float* coadis, int* stats,
+                                      cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (!f.ncand || !f.cand || f.cap <= 0) return cudaErrorInvalidValue;
+    const int kcap = pow2_ge(std::max(w, 2));
+    const int bcap = std::max(std::max(f.cap, 2 * CC_NT), kcap);
+    if (bcap & (bcap - 1)) return cudaErrorInvalidValue;  // the buffer is a power of two
+    const size_t sm = cand_select_smem(w, f.cap, ix.d);
+    if (sm > 200 * 1024) return cudaErrorNotSupported;
+    if (sm > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(coarse_cand_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    coarse_cand_select_kernel<<<nq, CC_NT, sm, st>>>(q, ix.d, ix.coa, ix.C, qnorm, ix.coa_norm, w, f, kcap, bcap,
+                                                      coaidx, coadis, stats);
+    return cudaGetLastError();
+}
+
+}  // namespace gbivf

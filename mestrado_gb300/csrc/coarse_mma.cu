@@ -21,7 +21,7 @@
 //     bound in the reference's exact FP32 arithmetic; the exact keyed top-w of
 //     those is the plain path's result, bit for bit.
 //
-// eps(q, c) = EPS_REL * ||q|| * ||c|| + 2^-20 (||q||^2 + ||c||^2) bounds the
+// eps(q, c) = MIXED_EPS_REL * ||q|| * ||c|| + 2^-20 (||q||^2 + ||c||^2) bounds the
 // distance error: the hi/lo split (|sum q_l (c~_l - c_l)| <= 2^-16 ||q|| ||c||),
 // an FP32 accumulator allowed to lose 4 ulps (2^-21) per addition over the
 // 2K = 256 products (every product of two BF16 values is exact in FP32),
@@ -46,7 +46,6 @@ constexpr int B_TILE_BYTES = 2 * B_HALF_BYTES;     // c_hi tile then c_lo tile
 constexpr uint32_t CORE_LBO = 128;                 // next core matrix along K
 constexpr uint32_t CORE_SBO = 2048;                // next 8-row group
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
-constexpr float EPS_REL = 2.0f * 2.0f * (1.52587890625e-05f + 256.0f * 4.76837158203125e-07f);
 
 // BF16 x BF16 -> F32, K-major A and B, M = 128, N = 128 (kind::f16 descriptor:
 // D format bits 4-5, A/B formats bits 7-9 / 10-12, N>>3 bits 17-22, M>>4 bits 24-28)
@@ -122,11 +121,13 @@ __global__ void bf16_split_tiles_kernel(const float* __restrict__ x, int n, int 
 
 // out != NULL: approximate distances, nq x C row-major. amin != NULL instead:
 // per (row, centroid tile) the smallest (distance, centroid) key, nq x gridDim.x.
+// flt.thr != NULL instead: per row, centroids with approx - eps <= thr are
+// appended to the row's candidates and those with approx + eps <= thr counted.
 __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restrict__ qtiles,
                                                          const uint8_t* __restrict__ ctiles, int nq, int C,
                                                          const double* __restrict__ qnorm,
                                                          const float* __restrict__ cnorm, float* __restrict__ out,
-                                                         unsigned long long* __restrict__ amin,
+                                                         unsigned long long* __restrict__ amin, CoarseFilter flt,
                                                          int* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* sA = sm;
@@ -197,6 +198,9 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
     if (ok) {
         const int row = qt * MM_M + warp * 32 + lane;
         const float qn = row < nq ? (float)qnorm[row] : 0.0f;
+        const float qlen = sqrtf(qn);
+        const float T = (flt.thr && row < nq) ? flt.thr[row] : 0.0f;
+        int below = 0;
         u64 best = KEY_MAX;
 #pragma unroll 1
         for (int ch = 0; ch < MM_N / 32; ch++) {
@@ -214,9 +218,30 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             const int c0 = ct * MM_N + ch * 32;
             if (amin) {
-                for (int j = 0; j < 32 && c0 + j < C; j++) {
-                    const u64 key = make_key(qn + cnorm[c0 + j] - 2.0f * __uint_as_float(r[j]), (uint32_t)(c0 + j));
-                    best = key < best ? key : best;
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    if (c0 + j < C) {
+                        const u64 key =
+                            make_key(qn + cnorm[c0 + j] - 2.0f * __uint_as_float(r[j]), (uint32_t)(c0 + j));
+                        best = key < best ? key : best;
+                    }
+                }
+            } else if (flt.thr) {
+                if (row < nq) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const int c = c0 + j;
+                        if (c < C) {
+                            const float cn = cnorm[c];
+                            const float a = qn + cn - 2.0f * __uint_as_float(r[j]);
+                            const float e = mixed_eps(qn, qlen, cn, flt.clen[c]);
+                            below += (a + e <= T) ? 1 : 0;
+                            if (a - e <= T) {
+                                const int slot = atomicAdd(&flt.ncand[row], 1);
+                                if (slot < flt.cap) flt.cand[(int64_t)row * flt.cap + slot] = c;
+                            }
+                        }
+                    }
                 }
             } else if (row < nq) {
                 float* o = out + (int64_t)row * C + c0;
@@ -231,11 +256,14 @@ __global__ void __launch_bounds__(128) coarse_mma_kernel(const uint8_t* __restri
                         *reinterpret_cast<float4*>(o + j) = v;
                     }
                 } else {
-                    for (int j = 0; j < 32 && c0 + j < C; j++) o[j] = qn + cnorm[c0 + j] - 2.0f * __uint_as_float(r[j]);
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        if (c0 + j < C) o[j] = qn + cnorm[c0 + j] - 2.0f * __uint_as_float(r[j]);
                 }
             }
         }
         if (amin && row < nq) amin[(int64_t)row * gridDim.x + ct] = best;
+        if (flt.thr && row < nq && below) atomicAdd(&flt.cnt[row], below);
     } else if (tid == 0) {
         atomicExch(err, 1);
     }
@@ -271,7 +299,7 @@ __global__ void __launch_bounds__(MS_NT) coarse_recheck_kernel(const float* __re
     const double qn = qnorm[qi];
     const float qlen = sqrtf((float)qn);
     for (int x = tid; x < MM_K; x += MS_NT) xq[x] = q[(int64_t)qi * MM_K + x];
-    auto eps_of = [&](int c) { return EPS_REL * qlen * clen[c] + 9.5367431640625e-07f * ((float)qn + cnorm[c]); };
+    auto eps_of = [&](int c) { return mixed_eps((float)qn, qlen, cnorm[c], clen[c]); };
     // pass 1: the w-th smallest upper bound
     topk_init(s, w);
     for (int i0 = 0; i0 < C; i0 += MS_NT * 8) {
@@ -340,7 +368,21 @@ cudaError_t launch_coarse_mma(const uint8_t* qtiles, const uint8_t* ctiles, int 
     cudaError_t e = cudaFuncSetAttribute(coarse_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     dim3 grid((C + MM_N - 1) / MM_N, (nq + MM_M - 1) / MM_M);
-    coarse_mma_kernel<<<grid, 128, sm, st>>>(qtiles, ctiles, nq, C, qnorm, cnorm, amin ? nullptr : out, amin, err);
+    coarse_mma_kernel<<<grid, 128, sm, st>>>(qtiles, ctiles, nq, C, qnorm, cnorm, amin ? nullptr : out, amin,
+                                              CoarseFilter{}, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_mma_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
+                                     const double* qnorm, const float* cnorm, const CoarseFilter& f, int* err,
+                                     cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (!f.thr || !f.cnt || !f.ncand || !f.cand || !f.clen || f.cap <= 0) return cudaErrorInvalidValue;
+    const size_t sm = A_TILE_BYTES + B_TILE_BYTES + 64;
+    cudaError_t e = cudaFuncSetAttribute(coarse_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid((C + MM_N - 1) / MM_N, (nq + MM_M - 1) / MM_M);
+    coarse_mma_kernel<<<grid, 128, sm, st>>>(qtiles, ctiles, nq, C, qnorm, cnorm, nullptr, nullptr, f, err);
     return cudaGetLastError();
 }
 

@@ -57,7 +57,8 @@ constexpr int CD_TILE = 64, CD_K = 32;
 
 __global__ void __launch_bounds__(256) coarse_dist_kernel(
     const float* __restrict__ X, int nq, const float* __restrict__ Cc, int C, int d,
-    const double* __restrict__ qnorm, const float* __restrict__ cnorm, float* __restrict__ out) {
+    const double* __restrict__ qnorm, const float* __restrict__ cnorm, float* __restrict__ out,
+    CoarseFilter flt) {
     __shared__ float Xs[CD_K][CD_TILE + 1];
     __shared__ float Cs[CD_K][CD_TILE + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -97,6 +98,20 @@ __global__ void __launch_bounds__(256) coarse_dist_kernel(
         if (q >= nq) continue;
         double qn = qnorm[q];
 #pragma unroll
+        if (flt.thr) {
+            // filtered: append the centroids within the query's bound
+            const float T = flt.thr[q];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                int c = c0 + tx + 16 * j;
+                if (c < C && expansion_from(qn, cnorm[c], acc[i][j]) <= T) {
+                    const int slot = atomicAdd(&flt.ncand[q], 1);
+                    if (slot < flt.cap) flt.cand[(int64_t)q * flt.cap + slot] = c;
+                }
+            }
+            continue;
+        }
+#pragma unroll
         for (int j = 0; j < 4; j++) {
             int c = c0 + tx + 16 * j;
             if (c < C) out[(int64_t)q * C + c] = expansion_from(qn, cnorm[c], acc[i][j]);
@@ -108,7 +123,16 @@ cudaError_t launch_coarse_dist(const DevIndex& ix, const float* q, const double*
                                float* out, cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
     dim3 grid((ix.C + CD_TILE - 1) / CD_TILE, (nq + CD_TILE - 1) / CD_TILE);
-    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, out);
+    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, out, CoarseFilter{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const double* qnorm, int nq,
+                                      const CoarseFilter& f, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (!f.thr || !f.ncand || !f.cand || f.cap <= 0) return cudaErrorInvalidValue;
+    dim3 grid((ix.C + CD_TILE - 1) / CD_TILE, (nq + CD_TILE - 1) / CD_TILE);
+    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, nullptr, f);
     return cudaGetLastError();
 }
 

@@ -103,6 +103,46 @@ cudaError_t launch_coarse_recheck(const float* approx, int nq, int C, int w, con
                                   float* coadis, int* ncand, cudaStream_t st);
 constexpr int MMA_QUERY_TILE = 128;
 
+// Error bound of the BF16-split coarse distances (derivation in coarse_mma.cu):
+// |approx - exact| <= mixed_eps(||q||^2, ||q||, ||c||^2, ||c||).
+constexpr float MIXED_EPS_REL = 2.0f * 2.0f * (1.52587890625e-05f + 256.0f * 4.76837158203125e-07f);
+__device__ __forceinline__ float mixed_eps(float qn, float qlen, float cn, float cl) {
+    return MIXED_EPS_REL * qlen * cl + 9.5367431640625e-07f * (qn + cn);
+}
+
+// Filtered coarse stage for large C (coarse_filter.cu). Per query a bound
+// thr[q] is taken from a sample of the centroids; the full pass appends every
+// centroid that can beat it to the query's candidate slots and counts the
+// centroids certainly within it; the exact keyed top-w is then taken over the
+// candidates, or over all C when the count shows the bound was too low.
+struct CoarseFilter {
+    const float* thr = nullptr;  // nq: bound of each query
+    int* cnt = nullptr;          // nq: centroids whose distance is certainly <= thr (NULL: = ncand)
+    int* ncand = nullptr;        // nq: candidates appended (may exceed cap; only cap are stored)
+    int32_t* cand = nullptr;     // nq x cap candidate centroids
+    int cap = 0;
+    const float* clen = nullptr;  // mixed form: centroid lengths (||c|| rounded up)
+};
+// sample size, rank and candidate capacity of the filtered stage; false when
+// the plain select over the full distance block is used instead
+bool coarse_filter_shape(int C, int w, int d, int* S, int* r, int* cap);
+// the plain form's pass: exact distances (as launch_coarse_dist) filtered by f
+cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const double* qnorm, int nq,
+                                      const CoarseFilter& f, cudaStream_t st);
+// the mixed form's pass: tcgen05 approximate distances filtered by f
+cudaError_t launch_coarse_mma_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
+                                     const double* qnorm, const float* cnorm, const CoarseFilter& f, int* err,
+                                     cudaStream_t st);
+// thr[q] = r-th smallest of a nq x S block of distances (clen != NULL: of the
+// upper bounds approx + mixed_eps)
+cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, const double* qnorm,
+                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st);
+// exact keyed top-w per query from the candidates of f (stats[0] += candidates
+// re-checked, stats[1] += queries that fell back to all C centroids)
+cudaError_t launch_coarse_cand_select(const DevIndex& ix, const float* q, const double* qnorm, int nq, int w,
+                                      const CoarseFilter& f, int32_t* coaidx, float* coadis, int* stats,
+                                      cudaStream_t st);
+
 // index building (build_gpu.cu); synchronous, allocate their own temporaries
 cudaError_t assign_rows(const float* x, int64_t n, int64_t ld, int d, const float* cent, int k, int32_t* assign,
                         cudaStream_t st);

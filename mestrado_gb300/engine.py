@@ -148,18 +148,21 @@ class GpuIndex:
         check(self.lib.gbivf_last_stage_ms(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def coarse_assign(self, queries, w, mixed=False, stats=False):
+    def coarse_assign(self, queries, w, mixed=False, stats=False, full=False):
         """knn_full over the coarse centroids: (coaidx, coadis) nq x w. With
-        mixed=True the tensor-core form runs (same results); stats=True also
-        returns the number of centroids it re-checked exactly."""
+        mixed=True the tensor-core form runs, with full=True the full-block
+        selection instead of the large-C filter (same results either way);
+        stats=True also returns the number of centroids re-checked exactly and
+        the number of queries that took all centroids exactly."""
         q = _c(queries, np.float32)
         nq = q.shape[0]
         idx = np.empty((nq, w), np.int32)
         dis = np.empty((nq, w), np.float32)
-        nc = C.c_int64(0)
-        flags = _lib.GBIVF_MIXED_COARSE if mixed else 0
+        nc, nf = C.c_int64(0), C.c_int64(0)
+        flags = (_lib.GBIVF_MIXED_COARSE if mixed else 0) | (_lib.GBIVF_COARSE_FULL if full else 0)
         check(self.lib.gbivf_coarse_assign_flags(self.h, _p(q), nq, w, flags, _p(idx), _p(dis), C.byref(nc)))
-        return (idx, dis, nc.value) if stats else (idx, dis)
+        check(self.lib.gbivf_last_coarse_stats(self.h, None, C.byref(nf)))
+        return (idx, dis, nc.value, nf.value) if stats else (idx, dis)
 
     def core_gpu(self, residual, rid_to_ivf, qid_to_starting_outid, nout, k, w):
         r = _c(residual, np.float32)

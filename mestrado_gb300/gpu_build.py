@@ -124,7 +124,10 @@ def exact_topk(base, queries, k: int, batch: int = 256):
     import torch
 
     torch.backends.cuda.matmul.allow_tf32 = False
-    bn = (base * base).sum(1)
+    bn = torch.empty(base.shape[0], dtype=torch.float32, device=base.device)
+    for r in range(0, base.shape[0], 1 << 22):
+        blk = base[r:r + (1 << 22)]
+        bn[r:r + len(blk)] = (blk * blk).sum(1)
     out = np.empty((queries.shape[0], k), np.int64)
     for s in range(0, queries.shape[0], batch):
         q = queries[s:s + batch]

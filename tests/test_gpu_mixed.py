@@ -27,7 +27,7 @@ def synthetic(C, nq, seed):
 
 def check_coarse(gi, q, w):
     a_idx, a_dis = gi.coarse_assign(q, w)
-    b_idx, b_dis, ncand = gi.coarse_assign(q, w, mixed=True, stats=True)
+    b_idx, b_dis, ncand, _ = gi.coarse_assign(q, w, mixed=True, stats=True)
     np.testing.assert_array_equal(b_idx, a_idx)
     np.testing.assert_array_equal(b_dis.view(np.uint32), a_dis.view(np.uint32))
     return ncand / len(q)
