@@ -12,6 +12,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <limits>
 #include <vector>
 
 #include "../../include/gbivf.h"
@@ -111,6 +112,7 @@ struct gbivf_index {
     bool mixed_pending = false;       // a coarse stage with device flags ran since the last flag check
     int64_t last_ncand = 0;           // centroids re-checked exactly by the last checked coarse stage
     int64_t last_fallbacks = 0;       // queries of it that took all C centroids exactly
+    float clen_max = 0.0f, cn_max = 0.0f;  // maxima of the centroid lengths / squared norms (mixed form)
     bool use_persistent = true;       // register-codebook scan where the shape allows
     int scan_threads = 512;           // block size of the persistent scan (512 or 1024)
     std::vector<void*> owned;    // index allocations
@@ -120,9 +122,9 @@ struct gbivf_index {
     // workspace
     DBuf w_q, w_qn, w_coaidx, w_coadis, w_cdist, w_ids, w_dis, w_res, w_start, w_queue, w_ckey, w_cid, w_ccnt;
     // mixed-precision coarse stage: centroid BF16 tiles, centroid lengths, query tiles, flags
-    DBuf coa_tiles, coa_len, w_qtiles, w_flags;
-    // filtered coarse stage (large C): per-query bounds, counters, candidate slots
-    DBuf w_thr, w_fcnt, w_cand;
+    DBuf coa_tiles, coa_len, coa_colG, coa_colK, w_qtiles, w_flags;
+    // filtered coarse stage (large C): per-query bounds, counters, candidate slots, GEMM survivors
+    DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
     bool ev_valid = false;
 };
@@ -145,8 +147,8 @@ void free_index(gbivf_index* ix) {
     ix->owned.clear();
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
-                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->w_qtiles, &ix->w_flags,
-                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand})
+                    &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
+                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -320,10 +322,35 @@ int prepare_mixed(gbivf_index* ix, cudaStream_t st) {
     std::vector<float> cn(dx.C);
     CK(cudaMemcpyAsync(cn.data(), dx.coa_norm, sizeof(float) * dx.C, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    for (int c = 0; c < dx.C; c++) len[c] = std::sqrt(cn[c]) * 1.0000002f;
+    // per-centroid columns of the persistent GEMM's pre-test and sample (coarse_gemm.cu)
+    const size_t ng = coarse_gemm_col_floats(dx.C);
+    std::vector<float> colG(ng, std::numeric_limits<float>::infinity()), colK(ng, 0.0f);
+    ix->clen_max = 0.0f;
+    ix->cn_max = 0.0f;
+    for (int c = 0; c < dx.C; c++) {
+        len[c] = std::sqrt(cn[c]) * 1.0000002f;
+        colG[c] = cn[c] * (1.0f - 9.5367431640625e-07f) * 0.5f;
+        colK[c] = MIXED_EPS_REL * len[c] * 0.5f;
+        ix->clen_max = std::max(ix->clen_max, len[c]);
+        ix->cn_max = std::max(ix->cn_max, cn[c]);
+    }
     CK(ix->coa_len.ensure(sizeof(float) * dx.C));
     CK(cudaMemcpyAsync(ix->coa_len.p, len.data(), sizeof(float) * dx.C, cudaMemcpyHostToDevice, st));
+    CK(ix->coa_colG.ensure(sizeof(float) * ng));
+    CK(cudaMemcpyAsync(ix->coa_colG.p, colG.data(), sizeof(float) * ng, cudaMemcpyHostToDevice, st));
+    CK(ix->coa_colK.ensure(sizeof(float) * ng));
+    CK(cudaMemcpyAsync(ix->coa_colK.p, colK.data(), sizeof(float) * ng, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
+    return GBIVF_OK;
+}
+
+// BF16 query tiles for the persistent GEMM: whole 256-row pairs, the unused
+// half of a last odd pair zeroed
+int make_query_tiles(gbivf_index* ix, const float* qb, int nb, cudaStream_t st) {
+    uint8_t* qt = ix->w_qtiles.as<uint8_t>();
+    CK(launch_bf16_tiles(qb, nb, MMA_QUERY_TILE, qt, st));
+    const size_t written = coarse_mma_tile_bytes(nb, false), total = coarse_gemm_qtile_bytes(nb);
+    if (total > written) CK(cudaMemsetAsync(qt + written, 0, total - written, st));
     return GBIVF_OK;
 }
 
@@ -339,7 +366,27 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
     CK(ix->w_thr.ensure(sizeof(float) * (size_t)bq));
     CK(ix->w_fcnt.ensure(2 * sizeof(int) * (size_t)bq));
     CK(ix->w_cand.ensure(sizeof(int32_t) * (size_t)bq * cap));
-    if (mixed) CK(ix->w_qtiles.ensure(coarse_mma_tile_bytes((int)bq, false)));
+    if (mixed) CK(ix->w_qtiles.ensure(coarse_gemm_qtile_bytes((int)bq)));
+    // mixed form: survivor regions of the GEMM, sized for about 4x the expected survivors
+    // (3w + 64 candidates spread evenly over the centroid ranges) and for the largest block
+    auto surv_shape = [&](int nb, int* nsplit, int* sreg) {
+        int st_tiles = 1;
+        *nsplit = coarse_gemm_nsplit(nb, dx.C, ix->num_sms, &st_tiles);
+        const double expect = (3.0 * w + 64.0) * (st_tiles * 128.0 / dx.C) / 2.0;
+        *sreg = std::min(4096, std::max(32, ((int)std::ceil(4.0 * expect) + 15) / 16 * 16));
+    };
+    if (mixed) {
+        size_t need_s = 0, need_c = 0;
+        for (int64_t nb : {bq, (int64_t)(nq % bq)}) {
+            if (nb <= 0) continue;
+            int ns, sr;
+            surv_shape((int)nb, &ns, &sr);
+            need_s = std::max(need_s, sizeof(int2) * (size_t)nb * 2 * ns * sr);
+            need_c = std::max(need_c, sizeof(int) * (size_t)nb * 2 * ns);
+        }
+        CK(ix->w_surv.ensure(need_s));
+        CK(ix->w_scnt.ensure(need_c));
+    }
     float* cd = ix->w_cdist.as<float>();
     float* thr = ix->w_thr.as<float>();
     int* cnt = ix->w_fcnt.as<int>();
@@ -358,13 +405,31 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
         CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int) * (size_t)bq, st));
         if (mixed) {
             uint8_t* qt = ix->w_qtiles.as<uint8_t>();
-            CK(launch_bf16_tiles(qb, nb, MMA_QUERY_TILE, qt, st));
-            CK(launch_coarse_mma(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, cd, fl, st));
-            CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, dx.coa_norm, ix->coa_len.as<float>(), thr, st));
-            CK(launch_coarse_mma_filter(qt, ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0, dx.coa_norm, f, fl, st));
+            int rc = make_query_tiles(ix, qb, nb, st);
+            if (rc) return rc;
+            const float* colG = ix->coa_colG.as<float>();
+            const float* colK = ix->coa_colK.as<float>();
+            if (r <= 128 && r <= S / 32) {
+                // sample: minima of 32-centroid chunks straight from the GEMM, bound from those
+                CK(launch_coarse_gemm_chunkmin(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, colG,
+                                               colK, cd, S / 32, ix->num_sms, fl, st));
+                CK(launch_coarse_sample_bound(cd, nb, S / 32, S / 32, r, thr, st));
+            } else {
+                CK(launch_coarse_gemm_store(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, cd, S,
+                                            ix->num_sms, fl, st));
+                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, dx.coa_norm, ix->coa_len.as<float>(), thr, st));
+            }
+            surv_shape(nb, &f.nsplit, &f.sreg);
+            f.surv = ix->w_surv.as<int2>();
+            f.scnt = ix->w_scnt.as<int>();
+            CK(launch_coarse_gemm_filter(qt, ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0, dx.coa_norm, f, colG,
+                                         colK, ix->cn_max, ix->clen_max, ix->num_sms, fl, st));
         } else {
             CK(launch_coarse_dist(sx, qb, qn + q0, nb, cd, st));
-            CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, nullptr, nullptr, thr, st));
+            if (r <= 128)
+                CK(launch_coarse_sample_bound(cd, nb, S, S, r, thr, st));
+            else
+                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, nullptr, nullptr, thr, st));
             CK(launch_coarse_dist_filter(dx, qb, qn + q0, nb, f, st));
         }
         CK(launch_coarse_cand_select(dx, qb, qn + q0, nb, w, f, coaidx + q0 * w, coadis + q0 * w, fl + 1, st));
@@ -415,16 +480,17 @@ int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, in
     int bq = coarse_batch(nq, dx.C);
     if (bq >= MMA_QUERY_TILE) bq = bq / MMA_QUERY_TILE * MMA_QUERY_TILE;
     CK(ix->w_cdist.ensure(sizeof(float) * (size_t)bq * dx.C));
-    CK(ix->w_qtiles.ensure(coarse_mma_tile_bytes(bq, false)));
+    CK(ix->w_qtiles.ensure(coarse_gemm_qtile_bytes(bq)));
     CK(ix->w_flags.ensure(4 * sizeof(int)));
     CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
     int* fl = ix->w_flags.as<int>();
     for (int q0 = 0; q0 < nq; q0 += bq) {
         int nb = std::min(bq, nq - q0);
         const float* qb = d_q + (int64_t)q0 * dx.d;
-        CK(launch_bf16_tiles(qb, nb, MMA_QUERY_TILE, ix->w_qtiles.as<uint8_t>(), st));
-        CK(launch_coarse_mma(ix->w_qtiles.as<uint8_t>(), ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0,
-                             dx.coa_norm, ix->w_cdist.as<float>(), fl, st));
+        int rc = make_query_tiles(ix, qb, nb, st);
+        if (rc) return rc;
+        CK(launch_coarse_gemm_store(ix->w_qtiles.as<uint8_t>(), ix->coa_tiles.as<uint8_t>(), nb, dx.C, qn + q0,
+                                    dx.coa_norm, ix->w_cdist.as<float>(), dx.C, ix->num_sms, fl, st));
         CK(launch_coarse_recheck(ix->w_cdist.as<float>(), nb, dx.C, w, qb, qn + q0, dx.coa, dx.coa_norm,
                                  ix->coa_len.as<float>(), coaidx + (int64_t)q0 * w, coadis + (int64_t)q0 * w, fl + 1,
                                  st));

@@ -33,7 +33,7 @@
 namespace gbivf {
 
 constexpr int KT_NT = 128, KT_ITEMS = 8;  // sample selection
-constexpr int CC_NT = 128;                // candidate selection
+constexpr int CC_NT = 128, CC_KC = 32;    // candidate selection: batch of rows, staged dimensions
 
 static int pow2_ge(int x) {
     int p = 2;
@@ -41,10 +41,13 @@ static int pow2_ge(int x) {
     return p;
 }
 
+constexpr int CC_MAX_REGIONS = 512;  // survivor regions per query (2 x the GEMM's centroid ranges)
+
 static size_t cand_select_smem(int w, int cap, int d) {
     const int kcap = pow2_ge(std::max(w, 2));
     const int bcap = std::max(std::max(cap, 2 * CC_NT), kcap);
-    return sizeof(u64) * (2 * (size_t)kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int) + sizeof(float) * d;
+    return sizeof(u64) * (2 * (size_t)kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int) + sizeof(float) * d +
+           sizeof(int) * CC_NT + sizeof(float) * CC_NT * (CC_KC + 1) + sizeof(int) * (CC_MAX_REGIONS + 4);
 }
 
 bool coarse_filter_shape(int C, int w, int d, int* S, int* r, int* cap) {
@@ -110,8 +113,40 @@ cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, co
     return cudaGetLastError();
 }
 
+constexpr int KB_NT = 512;  // sample bound: groups per query
+
+// thr[q] = r-th smallest of the minima of KB_NT interleaved groups of row q
+__global__ void __launch_bounds__(KB_NT) coarse_sample_bound_kernel(const float* __restrict__ vals, int L, int64_t ld,
+                                                                    int r, float* __restrict__ thr) {
+    __shared__ u64 keys[KB_NT];
+    __shared__ __align__(8) unsigned char work[TOPK_WORK_BYTES];
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const float* row = vals + (int64_t)q * ld;
+    float m = __int_as_float(0x7f800000);
+#pragma unroll 8
+    for (int c = tid; c < L; c += KB_NT) m = fminf(m, row[c]);
+    keys[tid] = make_key(m, (uint32_t)tid);
+    TopKSmem s{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, r, 0, 0, work};
+    if (tid == 0) s.slots()[0] = 0;
+    __syncthreads();
+    const u64 kth = block_kth(s, keys, KB_NT, keys, 0, r);
+    if (tid == 0) thr[q] = key_dist(kth);
+}
+
+cudaError_t launch_coarse_sample_bound(const float* vals, int nq, int L, int64_t ld, int r, float* thr,
+                                       cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (r < 1 || r > KB_NT / 4 || r > L || ld < L) return cudaErrorInvalidValue;
+    coarse_sample_bound_kernel<<<nq, KB_NT, 0, st>>>(vals, L, ld, r, thr);
+    return cudaGetLastError();
+}
+
 // Per query: exact keyed top-w over its candidates, or over all C centroids
-// when the candidates cannot be trusted to hold the w nearest.
+// when the candidates cannot be trusted to hold the w nearest. Candidates go
+// in batches of CC_NT, one per thread; their centroid rows are staged through
+// shared memory CC_KC dimensions at a time with row-contiguous (coalesced)
+// loads, and each thread keeps its own sequential dot product (l = 0..d-1,
+// the reference's order) across the chunks.
 __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* __restrict__ X, int d,
                                                                    const float* __restrict__ coa, int C,
                                                                    const double* __restrict__ qnorm,
@@ -127,34 +162,92 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
     unsigned char* work = reinterpret_cast<unsigned char*>(thresh + 1);
     int* cnt = reinterpret_cast<int*>(work + TOPK_WORK_BYTES);
     float* xq = reinterpret_cast<float*>(cnt + 2);
+    int* ids = reinterpret_cast<int*>(xq + d);
+    float* rows = reinterpret_cast<float*>(ids + CC_NT);  // [CC_NT][CC_KC + 1]
+    int* rcnt = reinterpret_cast<int*>(rows + CC_NT * (CC_KC + 1));  // [CC_MAX_REGIONS] survivor counts
+    int* tally = rcnt + CC_MAX_REGIONS;                               // candidates, below, overflow
     TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, work};
     const int q = blockIdx.x, tid = threadIdx.x;
     for (int l = tid; l < d; l += CC_NT) xq[l] = X[(int64_t)q * d + l];
     const double qn = qnorm[q];
-    const int n = f.ncand[q];
-    const int below = f.cnt ? f.cnt[q] : n;
-    const bool all = n > f.cap || below < w;
-    topk_init(s, w);  // (its barrier also publishes xq)
-    if (!all) {
-        // n <= cap <= bcap: every candidate fits the buffer, no flush until the end
-        const int32_t* cq = f.cand + (int64_t)q * f.cap;
-        for (int i0 = 0; i0 < n; i0 += CC_NT) {
-            const int i = i0 + tid;
-            u64 key = 0;
-            if (i < n) {
-                const int c = cq[i];
-                key = make_key(expansion_from(qn, cnorm[c], dot_seq(coa + (int64_t)c * d, xq, d)), (uint32_t)c);
+    int n, below;
+    bool overflow = false;
+    if (f.surv) {
+        // mixed form: the exact candidate (a - eps <= T) and count (a + eps <= T) tests on the
+        // GEMM's pre-test survivors; candidates go to this query's slots of f.cand
+        const int G = 2 * f.nsplit;
+        if (tid < 3) tally[tid] = 0;
+        for (int g = tid; g < G; g += CC_NT) {
+            int c = f.scnt[(int64_t)q * G + g];
+            if (c > f.sreg) {
+                tally[2] = 1;
+                c = f.sreg;
             }
-            topk_offer(s, key, i < n);
+            rcnt[g] = c;
         }
+        __syncthreads();
+        const float qf = (float)qn, qlen = sqrtf(qf), T = f.thr[q];
+        const int2* sq = f.surv + (int64_t)q * G * f.sreg;
+        int mine = 0;
+#pragma unroll 4
+        for (int e = tid; e < G * f.sreg; e += CC_NT) {
+            const int g = e / f.sreg, sl = e - g * f.sreg;
+            if (sl < rcnt[g]) {
+                const int2 v = sq[e];
+                const int c = v.x;
+                const float cn = cnorm[c];
+                const float a = qf + cn - 2.0f * __int_as_float(v.y);
+                const float ee = mixed_eps(qf, qlen, cn, f.clen[c]);
+                mine += (a + ee <= T) ? 1 : 0;
+                if (a - ee <= T) {
+                    const int slot = atomicAdd(&tally[0], 1);
+                    if (slot < f.cap) f.cand[(int64_t)q * f.cap + slot] = c;
+                }
+            }
+        }
+        if (mine) atomicAdd(&tally[1], mine);
+        __syncthreads();
+        n = tally[0];
+        below = tally[1];
+        overflow = tally[2] != 0;
     } else {
-        for (int i0 = 0; i0 < C; i0 += CC_NT) {
-            const int c = i0 + tid;
-            u64 key = 0;
-            if (c < C) key = make_key(expansion_from(qn, cnorm[c], dot_seq(coa + (int64_t)c * d, xq, d)), (uint32_t)c);
-            topk_offer(s, key, c < C);
-            topk_round_end(s, CC_NT);
+        n = f.ncand[q];
+        below = f.cnt ? f.cnt[q] : n;
+    }
+    const bool all = overflow || n > f.cap || below < w;
+    const int total = all ? C : n;  // without the fallback n <= cap <= bcap: no flush until the end
+    const int32_t* cq = f.cand + (int64_t)q * f.cap;
+    topk_init(s, w);  // (its barrier also publishes xq)
+    for (int i0 = 0; i0 < total; i0 += CC_NT) {
+        const int i = i0 + tid;
+        const bool valid = i < total;
+        const int c = valid ? (all ? i : cq[i]) : -1;
+        __syncthreads();  // the previous batch is done with ids / rows
+        ids[tid] = c;
+        __syncthreads();
+        float t = 0.0f;
+        for (int l0 = 0; l0 < d; l0 += CC_KC) {
+            const int lw = min(CC_KC, d - l0);
+            // all CC_KC loads of this thread in flight at once (warp = one row, lanes along it)
+            float v[CC_KC];
+#pragma unroll
+            for (int k = 0; k < CC_KC; k++) {
+                const int e = tid + k * CC_NT, rr = e / CC_KC, col = e % CC_KC;
+                const int cid = ids[rr];
+                v[k] = (cid >= 0 && col < lw) ? __ldg(coa + (int64_t)cid * d + l0 + col) : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < CC_KC; k++) {
+                const int e = tid + k * CC_NT, rr = e / CC_KC, col = e % CC_KC;
+                rows[rr * (CC_KC + 1) + col] = v[k];
+            }
+            __syncthreads();
+            for (int l = 0; l < lw; l++) t = __fadd_rn(t, __fmul_rn(rows[tid * (CC_KC + 1) + l], xq[l0 + l]));
+            __syncthreads();
         }
+        const u64 key = valid ? make_key(expansion_from(qn, cnorm[c], t), (uint32_t)c) : 0;
+        topk_offer(s, key, valid);
+        if (all) topk_round_end(s, CC_NT);
     }
     topk_finish(s);
     const int nb = *s.nbest;
@@ -163,7 +256,7 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
         coadis[(int64_t)q * w + j] = j < nb ? key_dist(best[j]) : __int_as_float(0x7f800000);
     }
     if (tid == 0 && stats) {
-        atomicAdd(&stats[0], all ? C : n);
+        atomicAdd(&stats[0], total);
         if (all) atomicAdd(&stats[1], 1);
     }
 }
@@ -172,7 +265,9 @@ cudaError_t launch_coarse_cand_select(const DevIndex& ix, const float* q, const 
                                       const CoarseFilter& f, int32_t* coaidx, float* coadis, int* stats,
                                       cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
-    if (!f.ncand || !f.cand || f.cap <= 0) return cudaErrorInvalidValue;
+    if (!f.cand || f.cap <= 0 || (!f.surv && !f.ncand)) return cudaErrorInvalidValue;
+    if (f.surv && (!f.scnt || !f.thr || !f.clen || f.sreg <= 0 || 2 * f.nsplit > CC_MAX_REGIONS))
+        return cudaErrorInvalidValue;
     const int kcap = pow2_ge(std::max(w, 2));
     const int bcap = std::max(std::max(f.cap, 2 * CC_NT), kcap);
     if (bcap & (bcap - 1)) return cudaErrorInvalidValue;  // the buffer is a power of two

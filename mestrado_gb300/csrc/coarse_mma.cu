@@ -36,56 +36,9 @@
 
 #include "block_topk.cuh"
 #include "kernels.cuh"
+#include "tc_common.cuh"
 
 namespace gbivf {
-
-constexpr int MM_M = 128, MM_N = 128, MM_K = 128;
-constexpr int A_TILE_BYTES = MM_M * MM_K * 2;      // 32 KB of queries
-constexpr int B_HALF_BYTES = MM_N * MM_K * 2;      // 32 KB: one of c_hi / c_lo
-constexpr int B_TILE_BYTES = 2 * B_HALF_BYTES;     // c_hi tile then c_lo tile
-constexpr uint32_t CORE_LBO = 128;                 // next core matrix along K
-constexpr uint32_t CORE_SBO = 2048;                // next 8-row group
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
-
-// BF16 x BF16 -> F32, K-major A and B, M = 128, N = 128 (kind::f16 descriptor:
-// D format bits 4-5, A/B formats bits 7-9 / 10-12, N>>3 bits 17-22, M>>4 bits 24-28)
-constexpr uint32_t MMA_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(MM_N >> 3) << 17) |
-                               ((uint32_t)(MM_M >> 4) << 24);
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: K-major, no swizzle, sm_100 version bits
-__device__ __forceinline__ uint64_t make_smem_desc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(CORE_LBO >> 4) << 16) |
-           ((uint64_t)(CORE_SBO >> 4) << 32) | (1ull << 46);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    const uint32_t a = smem_addr(bar);
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// element (row, k) of a K-major no-swizzle tile, in bytes (k-groups of 8 BF16)
-__host__ __device__ inline uint32_t tile_offset(int row, int k) {
-    return (uint32_t)(row >> 3) * CORE_SBO + (uint32_t)(k >> 3) * CORE_LBO + (uint32_t)(row & 7) * 16u +
-           (uint32_t)(k & 7) * 2u;
-}
 
 // rows of x (n x 128 float) -> BF16 tiles of `rows_per_tile` rows; rows past n are zero
 __global__ void bf16_tiles_kernel(const float* __restrict__ x, int n, int rows_per_tile, int padded,

@@ -122,6 +122,13 @@ struct CoarseFilter {
     int32_t* cand = nullptr;     // nq x cap candidate centroids
     int cap = 0;
     const float* clen = nullptr;  // mixed form: centroid lengths (||c|| rounded up)
+    // mixed form: the GEMM's pre-test survivors (centroid, accumulator bits),
+    // per (query, centroid range, column half) up to sreg each, with their
+    // counts (nq x 2*nsplit; a count above sreg means the region overflowed);
+    // the exact candidate and count tests run in launch_coarse_cand_select
+    int2* surv = nullptr;
+    int* scnt = nullptr;
+    int sreg = 0, nsplit = 0;
 };
 // sample size, rank and candidate capacity of the filtered stage; false when
 // the plain select over the full distance block is used instead
@@ -133,6 +140,34 @@ cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const 
 cudaError_t launch_coarse_mma_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
                                      const double* qnorm, const float* cnorm, const CoarseFilter& f, int* err,
                                      cudaStream_t st);
+// persistent pipelined tcgen05 coarse GEMM (coarse_gemm.cu); query tiles for
+// it hold coarse_gemm_qtile_bytes(nq) bytes (a multiple of two 128-row tiles);
+// per-centroid columns colG = ||c||^2 (1 - 2^-20) / 2 (+inf past C) and
+// colK = MIXED_EPS_REL ||c|| / 2 (0 past C) hold coarse_gemm_col_floats(C) floats
+size_t coarse_gemm_qtile_bytes(int nq);
+size_t coarse_gemm_col_floats(int C);
+// approximate distances nq x C (row stride ld)
+cudaError_t launch_coarse_gemm_store(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
+                                     const double* qnorm, const float* cnorm, float* out, int64_t ld, int num_sms,
+                                     int* err, cudaStream_t st);
+// per query and 32 centroids, about the smallest upper bound approx + eps: nq x C/32 (C % 32 == 0)
+cudaError_t launch_coarse_gemm_chunkmin(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
+                                        const double* qnorm, const float* cnorm, const float* colG,
+                                        const float* colK, float* out, int64_t ld, int num_sms, int* err,
+                                        cudaStream_t st);
+// centroid ranges per 256-query tile pair the persistent GEMM uses for (nq, C)
+int coarse_gemm_nsplit(int nq, int C, int num_sms, int* split_tiles);
+// the mixed form's filtered pass (f.surv / f.scnt / f.sreg / f.nsplit as above);
+// cn_max / clen_max: maxima of cnorm / f.clen
+cudaError_t launch_coarse_gemm_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
+                                      const double* qnorm, const float* cnorm, const CoarseFilter& f,
+                                      const float* colG, const float* colK, float cn_max, float clen_max,
+                                      int num_sms, int* err, cudaStream_t st);
+// thr[q] = a bound at about the r-th smallest of row q of a nq x L block (row
+// stride ld): the r-th smallest of the minima of 512 interleaved groups (so
+// at least r values lie at or below it); r <= 128 and r <= L
+cudaError_t launch_coarse_sample_bound(const float* vals, int nq, int L, int64_t ld, int r, float* thr,
+                                       cudaStream_t st);
 // thr[q] = r-th smallest of a nq x S block of distances (clen != NULL: of the
 // upper bounds approx + mixed_eps)
 cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, const double* qnorm,
