@@ -75,4 +75,21 @@ GB_HD float add_norms_rn(const double* Dp, float hi, float lo, float f) {
     return xr_d2f(xr_dadd(*Dp, (double)f));
 }
 
+#if defined(__CUDACC__)
+// the rounding decision of add_norms_rn, given S = RN32(hi + f) and t ~ (D + f) - S
+__device__ __forceinline__ float add_norms_finish(const double* Dp, float S, float t, float f) {
+    const uint32_t sb = __float_as_uint(S);
+    const uint32_t ex = sb & 0x7f800000u;
+    if ((sb & 0x007fffffu) != 0u && ex >= (64u << 23) && ex <= (200u << 23)) {
+        const float half = __uint_as_float(ex - (24u << 23));
+        const float eps = __uint_as_float(ex - (44u << 23));
+        const float up = __fsub_rn(t, half);
+        const float dn = __fadd_rn(t, half);
+        if (fabsf(up) > eps && fabsf(dn) > eps)
+            return up > 0.0f ? __uint_as_float(sb + 1u) : (dn < 0.0f ? __uint_as_float(sb - 1u) : S);
+    }
+    return __double2float_rn(__dadd_rn(*Dp, (double)f));
+}
+#endif
+
 }  // namespace gbivf

@@ -18,6 +18,7 @@
 // without block barriers. Results and the optional re-rank are shared with
 // the general kernel (scan_common.cuh).
 #include "exact_round.cuh"
+#include "f32x2.cuh"
 #include "scan_common.cuh"
 
 
@@ -180,6 +181,34 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                 }
                 const float f = DIRECT ? 0.0f : rn[jr * M + my_s];
                 float out[E];
+                if constexpr (E % 2 == 0 && !DIRECT) {
+                    // The dot products stay scalar: ptxas contracts a packed multiply and add into a
+                    // fused multiply-add, which rounds differently from the reference's separate
+                    // operations. The multiply-free TwoSum of the norm sum and the final -2 dot + c
+                    // (-2 dot is exact, so fusing it changes nothing) run on packed pairs.
+                    const f2_t f2 = f2_pack(f, f), m2 = f2_pack(-2.0f, -2.0f);
+#pragma unroll
+                    for (int i = 0; i < E; i += 2) {
+                        float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+                        for (int t = 0; t < DS; t++) {
+                            d0 = __fadd_rn(d0, __fmul_rn(rs[t], cen[i][t]));
+                            d1 = __fadd_rn(d1, __fmul_rn(rs[t], cen[i + 1][t]));
+                        }
+                        const f2_t hi2 = f2_pack(nhi[i], nhi[i + 1]);
+                        const f2_t S2 = f2_add(hi2, f2);
+                        const f2_t bb = f2_sub(S2, hi2);
+                        const f2_t e1 = f2_add(f2_sub(hi2, f2_sub(S2, bb)), f2_sub(f2, bb));
+                        const f2_t t2 = f2_add(e1, f2_pack(nlo[i], nlo[i + 1]));
+                        float Sa, Sb, ta, tb;
+                        f2_unpack(S2, Sa, Sb);
+                        f2_unpack(t2, ta, tb);
+                        const int e = my_s * KS + my_c0 + i;
+                        const f2_t c02 = f2_pack(add_norms_finish(ix.pq_norm + e, Sa, ta, f),
+                                                 add_norms_finish(ix.pq_norm + e + 1, Sb, tb, f));
+                        f2_unpack(f2_add(f2_mul(m2, f2_pack(d0, d1)), c02), out[i], out[i + 1]);
+                    }
+                } else
 #pragma unroll
                 for (int i = 0; i < E; i++) {
                     if (DIRECT) {
