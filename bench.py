@@ -482,6 +482,73 @@ def run_large(args, c, name, local_rank):
     gi.close()
 
 
+def run_coarse(args, c, name, local_rank):
+    """The coarse stage alone at a large configuration's shape (knn_full over C
+    centroids, w nearest per query): plain FP32 and tensor-core forms, timed
+    with CUDA events on device buffers. Centroids are mixture points plus
+    Gaussian noise (no k-means: the stage's cost does not depend on training)."""
+    import ctypes
+
+    import torch
+
+    from mestrado_gb300.engine import GpuIndex
+    from mestrado_gb300.gpu_build import GpuMixture
+    from mestrado_gb300.ivfdata import IVFPQData
+    from mestrado_gb300.synth import Mixture
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    gm = GpuMixture(Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"], zipf=c["zipf"]))
+    coa = gm.generate(c["C"], stream_id=5)
+    coa += torch.randn(coa.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(1)) * 2.0
+    q = gm.generate(c["nq"], stream_id=3)
+    m = c["m"]
+    rng = np.random.default_rng(0)
+    ix = IVFPQData(coa=coa.cpu().numpy(), pq=rng.normal(0, 10, (m, 256, c["d"] // m)).astype(np.float32),
+                   list_off=np.zeros(c["C"] + 1, np.int64), ids=np.zeros(0, np.int32),
+                   codes=np.zeros((0, m), np.uint8))
+    gi = GpuIndex(ix, device=local_rank)
+    nq, w = c["nq"], c["w"]
+    out_i = torch.empty((nq, w), dtype=torch.int32, device=dev)
+    out_d = torch.empty((nq, w), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    forms = {}
+    for form, flags in (("plain", 0), ("mixed", 0x4)):
+        ts = []
+        for i in range(args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xff)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            check_rc(gi.lib.gbivf_coarse_assign_device(gi.h, ctypes.c_void_p(q.data_ptr()), nq, w, flags,
+                                                       ctypes.c_void_p(out_i.data_ptr()),
+                                                       ctypes.c_void_p(out_d.data_ptr()),
+                                                       ctypes.c_void_p(stream.cuda_stream)), gi)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            if i >= args.warmup:
+                ts.append(e0.elapsed_time(e1))
+        forms[form] = dict(ms=float(np.median(ts)), ids=out_i.cpu().numpy())
+    same = bool(np.array_equal(forms["plain"]["ids"], forms["mixed"]["ids"]))
+    flops = 2.0 * nq * c["C"] * c["d"]
+    line = {"metric": "coarse-stage time", "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+            "config": {"workload": f"{name} coarse stage: {nq:,} queries x C={c['C']:,} centroids (d=128), w={w}",
+                       "l2": "flushed between steps (256 MB write)"},
+            "plain_ms": forms["plain"]["ms"], "mixed_ms": forms["mixed"]["ms"],
+            "speedup": forms["plain"]["ms"] / forms["mixed"]["ms"], "identical_lists": same,
+            "coarse_tflops_mixed": flops / (forms["mixed"]["ms"] / 1000.0) / 1e12}
+    print(json.dumps(line), flush=True)
+    gi.close()
+
+
+def check_rc(rc, gi):
+    if rc != 0:
+        raise RuntimeError(f"gbivf error {rc}: {gi.lib.gbivf_last_error().decode()}")
+
+
 def C_ptr(t):
     import ctypes
 
@@ -504,6 +571,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=10_000, help="queries per CPU step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
+    ap.add_argument("--stage", default="search", choices=["search", "coarse"],
+                    help="large configurations: time the whole search, or the coarse stage alone")
     args = ap.parse_args()
     if args.warmup < 3:
         log(f"--warmup {args.warmup} raised to 3 (at least 3 untimed warm-up steps)")
@@ -517,7 +586,10 @@ def main():
                 print(json.dumps({"impl": args.impl, "unavailable": "the large configurations run the GPU engine "
                                   "alone, on one GPU (the CPU oracle over 10M-100M vectors takes hours)"}))
             return
-        run_large(args, LARGE[args.config], args.config, local_rank)
+        if args.stage == "coarse":
+            run_coarse(args, LARGE[args.config], args.config, local_rank)
+        else:
+            run_large(args, LARGE[args.config], args.config, local_rank)
         return
     c = CONFIGS[args.config]
     if args.impl == "reference":

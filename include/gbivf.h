@@ -185,6 +185,13 @@ int gbivf_coarse_assign_noalloc(gbivf_index *ix, const float *d_queries, int nq,
 int gbivf_coarse_assign_flags(gbivf_index *ix, const float *queries, int nq, int w, unsigned flags,
                               int32_t *coaidx, float *coadis, int64_t *ncand);
 
+/* The coarse stage on device buffers, enqueued on `stream` (returns after
+ * launching; allocates workspace on first use): d_coaidx / d_coadis nq x w.
+ * flags: GBIVF_MIXED_COARSE, GBIVF_COARSE_FULL. A device-side timeout of the
+ * tensor-core form is reported by the next synchronous call on the index. */
+int gbivf_coarse_assign_device(gbivf_index *ix, const float *d_queries, int nq, int w, unsigned flags,
+                               int32_t *d_coaidx, float *d_coadis, void *stream);
+
 /* Work counters of the last gbivf_coarse_assign_flags call: centroids whose
  * distance was computed exactly after the first pass (the candidates of the
  * mixed form or of the large-C filter) and queries for which the large-C

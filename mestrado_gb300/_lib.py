@@ -27,7 +27,7 @@ EXPORTS = [
     "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc", "gbivf_coarse_assign_flags",
     "gbivf_search_batched", "gbivf_search_batched_device", "gbivf_graph_capture", "gbivf_graph_launch",
     "gbivf_graph_destroy", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
-    "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats",
+    "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats", "gbivf_coarse_assign_device",
 ]
 
 
@@ -66,6 +66,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
     lib.gbivf_coarse_assign_flags.argtypes = [vp, vp, i32, i32, u32, vp, vp, vp]
     lib.gbivf_last_coarse_stats.argtypes = [vp, vp, vp]
+    lib.gbivf_coarse_assign_device.argtypes = [vp, vp, i32, i32, u32, vp, vp, vp]
     lib.gbivf_search_batched.argtypes = [vp, vp, i32, vp, vp, u32, vp, vp]
     lib.gbivf_search_batched_device.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, u32, vp, vp, vp]
     lib.gbivf_graph_capture.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]

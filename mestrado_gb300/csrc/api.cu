@@ -979,6 +979,24 @@ int gbivf_coarse_assign_flags(gbivf_index* ix, const float* queries, int nq, int
     return rc;
 }
 
+int gbivf_coarse_assign_device(gbivf_index* ix, const float* d_queries, int nq, int w, unsigned flags,
+                               int32_t* d_coaidx, float* d_coadis, void* stream) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (w <= 0 || w > ix->dx.C || w > MAX_W) return fail(GBIVF_ERR_INVALID, "w=%d", w);
+    if (flags & ~(GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL)) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
+    if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
+    if (nq == 0) return GBIVF_OK;
+    if (!d_queries || !d_coaidx || !d_coadis) return fail(GBIVF_ERR_INVALID, "NULL device buffer");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(ix->w_qn.ensure(sizeof(double) * nq));
+    CK(launch_norm_d(d_queries, nq, ix->dx.d, ix->w_qn.as<double>(), st));
+    return coarse_stage(ix, d_queries, ix->w_qn.as<double>(), nq, w, flags, d_coaidx, d_coadis, st);
+}
+
 int gbivf_last_coarse_stats(gbivf_index* ix, int64_t* rechecked, int64_t* fallback_queries) {
     if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
     if (rechecked) *rechecked = ix->last_ncand;
