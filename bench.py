@@ -422,8 +422,8 @@ def run_large(args, c, name, local_rank):
     forms = {}
     for form, mixed in (("plain", False), ("mixed", True)):
         graph = gi.capture_graph(queries.data_ptr(), nq, max_k, max_w, d_ids.data_ptr(), d_dis.data_ptr(),
-                                 mixed_coarse=mixed, d_w_ptr=d_w.data_ptr(), d_k_ptr=d_k.data_ptr(),
-                                 d_off_ptr=d_off.data_ptr(), stream_ptr=sp)
+                                 mixed_coarse=mixed, mixed_scan=mixed, d_w_ptr=d_w.data_ptr(),
+                                 d_k_ptr=d_k.data_ptr(), d_off_ptr=d_off.data_ptr(), stream_ptr=sp)
         for i in range(args.warmup):
             graph.launch(sp)
         stream.synchronize()
@@ -446,14 +446,26 @@ def run_large(args, c, name, local_rank):
         ids = d_ids.cpu().numpy()
         # stage split from one profiled (non-graph) run
         gi.lib.gbivf_search_batched_device(gi.h, C_ptr(queries), nq, C_ptr(d_w), C_ptr(d_k), C_ptr(d_off),
-                                           max_w, max_k, 0x100 | (0x4 if mixed else 0), C_ptr(d_ids),
+                                           max_w, max_k, 0x100 | (0x14 if mixed else 0), C_ptr(d_ids),
                                            C_ptr(d_dis), sp_ptr(sp))
         cm, sm = gi.last_stage_ms()
         rec = [len(set(ids[off[i]:off[i] + kq[i]].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i]
                for i in range(sample)]
         forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps,
-                           coarse_ms=cm, scan_ms=sm, recall=float(np.mean(rec)), clocks=clk, ids=ids)
-    same = bool(np.array_equal(forms["plain"]["ids"], forms["mixed"]["ids"]))
+                           coarse_ms=cm, scan_ms=sm, recall=float(np.mean(rec)), clocks=clk, ids=ids,
+                           dis=d_dis.cpu().numpy())
+    pi, mi = forms["plain"]["ids"], forms["mixed"]["ids"]
+    same_rows = float(np.mean([np.array_equal(pi[off[i]:off[i + 1]], mi[off[i]:off[i + 1]]) for i in range(nq)]))
+    overlap = float(np.mean([len(set(pi[off[i]:off[i + 1]].tolist()) & set(mi[off[i]:off[i + 1]].tolist())) / kq[i]
+                             for i in range(nq)]))
+    # every distance the mixed form returns for an id the plain form also returns must be identical
+    pd_, md_ = forms["plain"]["dis"], forms["mixed"]["dis"]
+    mismatch = 0
+    for i in range(nq):
+        a = dict(zip(pi[off[i]:off[i + 1]].tolist(), pd_[off[i]:off[i + 1]].view(np.uint32).tolist()))
+        for idv, dv in zip(mi[off[i]:off[i + 1]].tolist(), md_[off[i]:off[i + 1]].view(np.uint32).tolist()):
+            mismatch += int(idv in a and a[idv] != dv)
+    same = same_rows == 1.0
     peak, peak_kind = measured_peak_hbm()
     mx = forms["mixed"]
     achieved = scan_bytes / (mx["scan_ms"] / 1000.0) / 1e9
@@ -464,10 +476,14 @@ def run_large(args, c, name, local_rank):
     line = {
         "metric": "QPS", "value": mx["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (coarse on bf16 tensor cores + fp32 re-check)", "data": "synthetic",
-        "config": {"workload": wl, "form": "mixed (tensor-core coarse stage), CUDA-graph replay",
+        "vs_baseline": None, "dtype": "bf16 tensor-core coarse + fp32 re-check; fp16 tables, fp32 re-score",
+        "data": "synthetic",
+        "config": {"workload": wl, "form": "mixed: tensor-core coarse stage and fp16-table scan with the "
+                   f"{4}k best re-scored in fp32; CUDA-graph replay",
                    "plain_qps": forms["plain"]["qps"], "speedup_vs_plain": mx["qps"] / forms["plain"]["qps"],
-                   "identical_ids_plain_vs_mixed": same, f"recall_sample_queries": sample,
+                   "identical_ids_plain_vs_mixed": same, "identical_rows_fraction": same_rows,
+                   "id_overlap_with_plain": overlap, "distance_mismatches_on_shared_ids": mismatch,
+                   f"recall_sample_queries": sample,
                    "recall_mixed": mx["recall"], "recall_plain": forms["plain"]["recall"],
                    "stage_ms_mixed": {"coarse": mx["coarse_ms"], "scan": mx["scan_ms"]},
                    "stage_ms_plain": {"coarse": forms["plain"]["coarse_ms"], "scan": forms["plain"]["scan_ms"]},

@@ -15,6 +15,7 @@ GBIVF_RERANK = 0x1
 GBIVF_TABLE_DIRECT = 0x2
 GBIVF_MIXED_COARSE = 0x4
 GBIVF_COARSE_FULL = 0x8
+GBIVF_MIXED_SCAN = 0x10
 GBIVF_PROFILE = 0x100
 
 _lib = None

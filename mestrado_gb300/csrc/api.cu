@@ -125,6 +125,8 @@ struct gbivf_index {
     DBuf coa_tiles, coa_len, coa_colG, coa_colK, w_qtiles, w_flags;
     // filtered coarse stage (large C): per-query bounds, counters, candidate slots, GEMM survivors
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
+    // precision form of the scan: per-list table terms (C x m x 256), hand-off lists
+    DBuf term2, w_clist;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
     bool ev_valid = false;
 };
@@ -148,7 +150,7 @@ void free_index(gbivf_index* ix) {
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
-                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt})
+                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->term2, &ix->w_clist})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -276,7 +278,22 @@ int coarse_batch(int nq, int C) {
 int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
-    if (ix->use_persistent && scan_persistent_supported(ix->dx, a)) {
+    const bool mixed = a.flags & SCAN_MIXED;
+    if (mixed) {
+        // precision form: per-list table terms, built once per index
+        if (!ix->term2.p) {
+            const DevIndex& dx = ix->dx;
+            CK(ix->term2.ensure(sizeof(float) * (size_t)dx.C * dx.m * dx.ks));
+            CK(launch_term2(dx, ix->term2.as<float>(), st));
+        }
+        a.term2 = ix->term2.as<float>();
+        a.sel_mult = GBIVF_MIXED_SCAN_ALPHA;
+        a.sel_cap = 4096;
+        if (!scan_persistent_supported(ix->dx, a))
+            return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN needs d = 128, ks = 256, m in {4, 8, 16} and "
+                                               "k (or kl) <= 1024");
+    }
+    if (mixed || (ix->use_persistent && scan_persistent_supported(ix->dx, a))) {
         const int stride = scan_persistent_stride(a);
         CK(ix->w_ckey.ensure(sizeof(unsigned long long) * (size_t)a.nq * stride));
         CK(ix->w_cid.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
@@ -285,6 +302,10 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
         a.cand_id = ix->w_cid.as<int32_t>();
         a.cand_cnt = ix->w_ccnt.as<int32_t>();
         a.cand_stride = stride;
+        if (mixed) {
+            CK(ix->w_clist.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
+            a.cand_list = ix->w_clist.as<int32_t>();
+        }
         CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st));
     } else {
         CK(launch_scan(ix->dx, a, st));
@@ -298,8 +319,11 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (k <= 0 || k > MAX_K) return fail(k <= 0 ? GBIVF_ERR_INVALID : GBIVF_ERR_UNSUPPORTED, "k=%d (1..%d)", k, MAX_K);
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
-    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL))
+    if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL |
+                  GBIVF_MIXED_SCAN))
         return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_TABLE_DIRECT))
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN uses the expansion tables (not GBIVF_TABLE_DIRECT)");
     if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
     if (flags & GBIVF_RERANK) {
@@ -541,7 +565,8 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.w = w;
     a.k = k;
     a.kl = kl;
-    a.flags = (flags & GBIVF_RERANK ? SCAN_RERANK : 0) | (flags & GBIVF_TABLE_DIRECT ? SCAN_TABLE_DIRECT : 0);
+    a.flags = (flags & GBIVF_RERANK ? SCAN_RERANK : 0) | (flags & GBIVF_TABLE_DIRECT ? SCAN_TABLE_DIRECT : 0) |
+              (flags & GBIVF_MIXED_SCAN ? SCAN_MIXED : 0);
     a.queries = d_q;
     a.qnorm = qn;
     a.probes = coaidx;

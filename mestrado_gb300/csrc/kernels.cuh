@@ -11,6 +11,7 @@ enum ScanFlags : int {
     SCAN_TABLE_DIRECT = 2,  // tables as sum (r-c)^2 (parallel2 core)
     SCAN_SRC_RESIDUAL = 4,  // residuals are given (nq*w x d) instead of queries
     SCAN_OUT_PACKED = 8,    // write min(L, k) results at out_start[q] (core_gpu)
+    SCAN_MIXED = 16,        // precision form: FP16 approximate tables, exact re-score of alpha*k
 };
 
 // Device view of one index (all pointers in device memory).
@@ -53,6 +54,12 @@ struct ScanArgs {
     const int32_t* w_per_q = nullptr;
     const int32_t* k_per_q = nullptr;
     const int64_t* out_off = nullptr;
+    // precision form (SCAN_MIXED): per-list table terms term2[l][s][c] = ||c||^2 + 2 <y_{l,s}, c>
+    // (C x m x 256), the approximate selection size min(sel_mult * k, sel_cap), and the hand-off's
+    // list of each candidate (cand_id then holds its code row)
+    const float* term2 = nullptr;
+    int sel_mult = 1, sel_cap = 0;
+    int32_t* cand_list = nullptr;
 };
 
 // per-query shape of a (possibly uneven) batch
@@ -87,6 +94,9 @@ cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int nu
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
+
+// precision form of the scan: term2[l][s][c] = ||c||^2 + 2 <y_{l,s}, c> for every list (C x m x ks)
+cudaError_t launch_term2(const DevIndex& ix, float* term2, cudaStream_t st);
 
 // mixed-precision coarse stage (d = 128): BF16 tiles, tcgen05 GEMM, exact re-check
 cudaError_t launch_bf16_tiles(const float* x, int n, int rows_per_tile, uint8_t* out, cudaStream_t st);

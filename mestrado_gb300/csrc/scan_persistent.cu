@@ -17,6 +17,8 @@
 // made once per list at a barrier that exists anyway, and the scan loop runs
 // without block barriers. Results and the optional re-rank are shared with
 // the general kernel (scan_common.cuh).
+#include <cuda_fp16.h>
+
 #include "exact_round.cuh"
 #include "f32x2.cuh"
 #include "scan_common.cuh"
@@ -52,7 +54,35 @@ __device__ __forceinline__ float adc_sum(uint4 v, const float* T) {
     return adc4(adc4(adc4(adc4(0.0f, v.x, T), v.y, T + 1024), v.z, T + 2048), v.w, T + 3072);
 }
 
-template <int M, bool DIRECT, int NT>
+// Precision form of the scan: approximate tables held in FP16 (scaled by 2^-2
+// so that partial distances up to 2^18 fit; saturating), summed in FP32 with the
+// mixed-precision add (add.rn.f32.f16, sm_100 and later), scaled back by 4.
+constexpr float SP_T16_SCALE = 0.25f;
+
+__device__ __forceinline__ float add_f16(float acc, const __half* p) {
+    const unsigned short h = *reinterpret_cast<const unsigned short*>(p);
+    asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc) : "h"(h));
+    return acc;
+}
+__device__ __forceinline__ float adc4h(float acc, uint32_t v, const __half* T) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) acc = add_f16(acc, T + s * 256 + ((v >> (8 * s)) & 0xff));
+    return acc;
+}
+__device__ __forceinline__ float adc_sum16(uint32_t v, const __half* T) { return adc4h(0.0f, v, T) * 4.0f; }
+__device__ __forceinline__ float adc_sum16(uint2 v, const __half* T) {
+    return adc4h(adc4h(0.0f, v.x, T), v.y, T + 1024) * 4.0f;
+}
+__device__ __forceinline__ float adc_sum16(uint4 v, const __half* T) {
+    return adc4h(adc4h(adc4h(adc4h(0.0f, v.x, T), v.y, T + 1024), v.z, T + 2048), v.w, T + 3072) * 4.0f;
+}
+__device__ __forceinline__ unsigned short f16_sat(float x) {
+    unsigned short h;
+    asm("cvt.rn.satfinite.f16.f32 %0, %1;" : "=h"(h) : "f"(x));
+    return h;
+}
+
+template <int M, bool DIRECT, int NT, bool MIXED = false>
 __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap) {
     constexpr int D = 128, KS = 256, DS = D / M, E = M * KS / NT;
     constexpr int TPS = NT / M;  // threads per sub-quantizer
@@ -109,7 +139,9 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
         if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
         // this query's probe count and result count (uneven batches)
         const int wq = query_w(a, q);
-        const int kq = (a.flags & SCAN_RERANK) ? a.kl : query_k(a, q);
+        const int kq0 = (a.flags & SCAN_RERANK) ? a.kl : query_k(a, q);
+        // the precision form keeps alpha * k approximate candidates for the exact re-score
+        const int kq = MIXED ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
         if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
         // probe lists and their prefix sums, one warp
         if (tid < 32) {
@@ -135,6 +167,18 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             if (lane == 0) prefix[wq] = carry;
         }
         topk_init(s, kq);
+        // precision form: this thread's per-query table term q3[i] = -2 <x_s, c_i> (its E entries)
+        float q3[MIXED ? E : 1];
+        if constexpr (MIXED) {
+            const float* xs = xq + my_s * DS;
+#pragma unroll
+            for (int i = 0; i < E; i++) {
+                float dt = 0.0f;
+#pragma unroll
+                for (int t = 0; t < DS; t++) dt = __fmaf_rn(xs[t], cen[i][t], dt);
+                q3[i] = -2.0f * dt;
+            }
+        }
 
         for (int j = 0; j < wq; j++) {
             const int jr = j % SP_RCH;
@@ -167,6 +211,27 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                 cur[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
             }
             float* table = tables + (j & 1) * (M * KS);
+            __half* table16 = reinterpret_cast<__half*>(tables) + (j & 1) * (M * KS);
+            if constexpr (MIXED) {
+                // approximate entry ||r_s - c||^2 = term2[l][s][c] + q3 + ||r_s||^2, where
+                // term2 = ||c||^2 + 2 <y_{l,s}, c> is precomputed per list: 2 adds per entry
+                const float f = rn[jr * M + my_s];
+                const float* t2 = a.term2 + ((int64_t)l * M + my_s) * KS + my_c0;
+                unsigned short h[E];
+#pragma unroll
+                for (int i = 0; i < E; i++) h[i] = f16_sat((__ldg(t2 + i) + q3[i] + f) * SP_T16_SCALE);
+                __half* dst = table16 + my_s * KS + my_c0;
+                if constexpr (E == 8) {
+                    *reinterpret_cast<uint4*>(dst) =
+                        make_uint4(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16,
+                                   h[4] | (uint32_t)h[5] << 16, h[6] | (uint32_t)h[7] << 16);
+                } else if constexpr (E == 4) {
+                    *reinterpret_cast<uint2*>(dst) = make_uint2(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < E; i++) reinterpret_cast<unsigned short*>(dst)[i] = h[i];
+                }
+            } else
             // table row segment from the register codebook
             {
                 float rs[DS];
@@ -267,7 +332,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     const int iw = i0 + u * NT + (tid & ~31);
                     if (iw < len) {
                         const int i = i0 + u * NT + tid;
-                        const float dist = adc_sum(cur[u], table);
+                        const float dist = MIXED ? adc_sum16(cur[u], table16) : adc_sum(cur[u], table);
                         const uint32_t pos = pos0 + (uint32_t)i;
                         const bool pass = i < len && (dist < td || (dist == td && pos < tp));
                         topk_push(s, make_key(dist, pos), pass);
@@ -295,10 +360,20 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const int64_t o = (int64_t)q * a.cand_stride + c;
             if (c < nbest) {
                 a.cand_key[o] = best[c];
-                a.cand_id[o] = pos_to_id(ix, prefix, plist, wq, key_payload(best[c]));
+                if constexpr (MIXED) {
+                    // the code row and its list, for the exact re-score
+                    const uint32_t pos = key_payload(best[c]);
+                    const int jj = probe_of(prefix, wq, pos);
+                    const int ll = plist[jj];
+                    a.cand_id[o] = (int32_t)(ix.list_beg[ll] + (int64_t)(pos - prefix[jj]));
+                    a.cand_list[o] = ll;
+                } else {
+                    a.cand_id[o] = pos_to_id(ix, prefix, plist, wq, key_payload(best[c]));
+                }
             } else {
                 a.cand_key[o] = KEY_MAX;
                 a.cand_id[o] = -1;
+                if constexpr (MIXED) a.cand_list[o] = 0;
             }
         }
         if (tid == 0) a.cand_cnt[q] = nbest;
@@ -330,6 +405,67 @@ __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
     }
 }
 
+// The reference's ADC distance of one code row of list l (d = 128, m = M), recomputed from scratch
+// in its arithmetic: per sub-quantizer the residual r_s = x_s - y_{l,s}, its float
+// norm, the sequential dot with the code's centroid, the norm sum and -2 dot + c
+// (compute_cross_distances, nn.c:113-150), summed in s order (sumidxtab2,
+// ivf_search.cpp:189-200). Bit-identical to the scan's exact table entries.
+template <int M>
+__device__ __forceinline__ float exact_adc(const DevIndex& ix, const float* xq, int l, int64_t row) {
+    constexpr int DS = 128 / M, H = M >= 8 ? M / 2 : M;  // sub-quantizers per batch of loads
+    using CT = typename CodeRow<M>::T;
+    const CT cr = load_row<M>(ix.codes + row * M);
+    const uint32_t* cw = reinterpret_cast<const uint32_t*>(&cr);
+    const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128);
+    float dist = 0.0f;
+#pragma unroll
+    for (int s0 = 0; s0 < M; s0 += H) {
+        // every load of this batch of sub-quantizers first, then the arithmetic
+        float4 yv[H * DS / 4], cv[H * DS / 4];
+        float hi[H], lo[H];
+        int ent[H];
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            const int s = s0 + h;
+            ent[h] = s * 256 + ((cw[s >> 2] >> (8 * (s & 3))) & 0xff);
+            const float4* c4 = reinterpret_cast<const float4*>(ix.pq + (int64_t)ent[h] * DS);
+#pragma unroll
+            for (int v = 0; v < DS / 4; v++) {
+                yv[h * (DS / 4) + v] = __ldg(y4 + s * (DS / 4) + v);
+                cv[h * (DS / 4) + v] = __ldg(c4 + v);
+            }
+            hi[h] = __ldg(ix.pq_hi + ent[h]);
+            lo[h] = __ldg(ix.pq_lo + ent[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            const int s = s0 + h;
+            float r[DS], cc[DS];
+#pragma unroll
+            for (int v = 0; v < DS / 4; v++) {
+                const float4 y = yv[h * (DS / 4) + v], c = cv[h * (DS / 4) + v];
+                r[4 * v] = __fsub_rn(xq[s * DS + 4 * v], y.x);
+                r[4 * v + 1] = __fsub_rn(xq[s * DS + 4 * v + 1], y.y);
+                r[4 * v + 2] = __fsub_rn(xq[s * DS + 4 * v + 2], y.z);
+                r[4 * v + 3] = __fsub_rn(xq[s * DS + 4 * v + 3], y.w);
+                cc[4 * v] = c.x;
+                cc[4 * v + 1] = c.y;
+                cc[4 * v + 2] = c.z;
+                cc[4 * v + 3] = c.w;
+            }
+            float f = 0.0f, dot = 0.0f;
+#pragma unroll
+            for (int t = 0; t < DS; t++) f = __fadd_rn(f, __fmul_rn(r[t], r[t]));
+#pragma unroll
+            for (int t = 0; t < DS; t++) dot = __fadd_rn(dot, __fmul_rn(r[t], cc[t]));
+            const float c0 = add_norms_rn(ix.pq_norm + ent[h], hi[h], lo[h], f);
+            dist = __fadd_rn(dist, __fadd_rn(__fmul_rn(-2.0f, dot), c0));
+        }
+    }
+    return dist;
+}
+
+template <bool MIXED, int M = 8>
 __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     const int n2 = a.cand_stride;  // power of two
@@ -337,16 +473,39 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
     float* xq = reinterpret_cast<float*>(ids + n2);
     const int q = blockIdx.x, tid = threadIdx.x;
-    const int n = a.cand_cnt[q];
-    for (int c = tid; c < n2; c += FIN_NT) {
+    int n = a.cand_cnt[q];
+    // only this query's candidates are sorted: the smallest power of two holding them (the
+    // hand-off pads with KEY_MAX), not the batch-wide stride
+    int p2 = 2;
+    while (p2 < n) p2 <<= 1;
+    for (int c = tid; c < p2; c += FIN_NT) {
         keys[c] = a.cand_key[(int64_t)q * n2 + c];
         ids[c] = a.cand_id[(int64_t)q * n2 + c];
     }
     const bool rerank = a.flags & SCAN_RERANK;
-    if (rerank)
+    if (rerank || MIXED)
         for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
     __syncthreads();
-    bitonic_sort_pairs(keys, ids, n2);
+    if constexpr (MIXED) {
+        // exact re-score of the alpha*k approximate candidates, keyed (distance, position) as
+        // the plain form keys them; the exact top-k (or top-kl) is then the plain form's
+        // whenever it lies among the candidates
+        for (int c = tid; c < p2; c += FIN_NT) {
+            u64 key = KEY_MAX;
+            if (c < n) {
+                const float dist = exact_adc<M>(ix, xq, a.cand_list[(int64_t)q * n2 + c], ids[c]);
+                key = make_key(dist, key_payload(keys[c]));
+            }
+            keys[c] = key;
+        }
+        __syncthreads();
+        bitonic_sort_pairs(keys, ids, p2);
+        for (int c = tid; c < n; c += FIN_NT) ids[c] = ix.ids[ids[c]];  // code rows -> base ids
+        __syncthreads();
+        n = min(n, rerank ? a.kl : query_k(a, q));
+    } else {
+        bitonic_sort_pairs(keys, ids, p2);
+    }
     const float inf = __int_as_float(0x7f800000);
     if (!rerank) {
         if (a.flags & SCAN_OUT_PACKED) {
@@ -368,7 +527,9 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     // exact distances of the n candidates in ADC order, keyed by that rank
     const double qn = a.qnorm[q];
     const int d = ix.d;
-    for (int c = tid; c < n2; c += FIN_NT) {
+    int pr = 2;
+    while (pr < n) pr <<= 1;
+    for (int c = tid; c < pr; c += FIN_NT) {
         u64 key = KEY_MAX;
         if (c < n) {
             const float4* v4 = reinterpret_cast<const float4*>(ix.base + (int64_t)ids[c] * d);
@@ -385,7 +546,7 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
         keys[c] = key;
     }
     __syncthreads();
-    bitonic_sort_smem(keys, n2);
+    bitonic_sort_smem(keys, pr);
     const int kq = query_k(a, q);
     const int64_t o = query_out(a, q);
     const int kr = min(kq, n);
@@ -398,21 +559,25 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
     const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
     const bool m_ok = ix.m == 4 || ix.m == 8 || ix.m == 16;
+    const bool mixed_ok = !(a.flags & SCAN_MIXED) ||
+                          !(a.flags & (SCAN_TABLE_DIRECT | SCAN_SRC_RESIDUAL | SCAN_OUT_PACKED));
     return ix.d == 128 && ix.ks == 256 && m_ok && std::max(kk, a.k) <= 1024 && a.queue != nullptr &&
-           ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK));
+           ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK)) && mixed_ok;
 }
 
 int scan_persistent_stride(const ScanArgs& a) {
     const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
-    return pow2_at_least(std::max(std::max(kk, a.k), 2));
+    const int sel = (a.flags & SCAN_MIXED) ? std::min(kk * a.sel_mult, a.sel_cap) : kk;
+    return pow2_at_least(std::max(std::max(sel, a.k), 2));
 }
 
-template <int M, bool DIRECT, int NT>
+template <int M, bool DIRECT, int NT, bool MIXED = false>
 static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
     const int kcap = scan_persistent_stride(a);
     if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
+    if (MIXED && (!a.term2 || !a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
     ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH);
-    auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT>;
+    auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT, MIXED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -426,17 +591,26 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t fsm = (size_t)kcap * (sizeof(u64) + sizeof(int32_t)) + sizeof(float) * 128;
+    auto fin = finalize_kernel<MIXED, M>;
     if (fsm > 48 * 1024) {
-        e = cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+        e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
         if (e != cudaSuccess) return e;
     }
-    finalize_kernel<<<a.nq, FIN_NT, fsm, st>>>(ix, a);
+    fin<<<a.nq, FIN_NT, fsm, st>>>(ix, a);
     return cudaGetLastError();
 }
 
 template <int NT>
 static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
     const bool direct = a.flags & SCAN_TABLE_DIRECT;
+    if (a.flags & SCAN_MIXED) {  // the precision form: 512 threads, expansion tables
+        if (direct) return cudaErrorNotSupported;
+        switch (ix.m) {
+            case 4: return launch_sp<4, false, 512, true>(ix, a, num_sms, st);
+            case 8: return launch_sp<8, false, 512, true>(ix, a, num_sms, st);
+            default: return launch_sp<16, false, 512, true>(ix, a, num_sms, st);
+        }
+    }
     switch (ix.m) {
         case 4: return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st) : launch_sp<4, false, NT>(ix, a, num_sms, st);
         case 8: return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st) : launch_sp<8, false, NT>(ix, a, num_sms, st);

@@ -81,7 +81,8 @@ class GpuIndex:
         return d.value, c.value, m.value, ks.value, n.value
 
     # -- searches ---------------------------------------------------------
-    def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False):
+    def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False,
+               mixed_scan=False):
         """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
         pass preallocated (ids, dis) host arrays (e.g. pinned memory)."""
         q = _c(queries, np.float32)
@@ -95,20 +96,22 @@ class GpuIndex:
             assert dis.shape == (nq, k) and dis.dtype == np.float32 and dis.flags.c_contiguous
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
+        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
         return ids, dis
 
     def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      stream_ptr=0, profile=False, mixed_coarse=False):
+                      stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False):
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
+        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
 
-    def search_batched(self, queries, w_per_q, k_per_q, mixed_coarse=False):
+    def search_batched(self, queries, w_per_q, k_per_q, mixed_coarse=False, mixed_scan=False):
         """Uneven batch: per-query nprobe and k. Returns (ids, dis, offsets):
         query q's results are ids[offsets[q]:offsets[q+1]]."""
         q = _c(queries, np.float32)
@@ -118,14 +121,15 @@ class GpuIndex:
         np.cumsum(kq, out=off[1:])
         ids = np.empty(int(off[-1]), np.int32)
         dis = np.empty(int(off[-1]), np.float32)
-        flags = _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
+        flags = (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0) | (_lib.GBIVF_MIXED_SCAN if mixed_scan else 0)
         check(self.lib.gbivf_search_batched(self.h, _p(q), q.shape[0], _p(wq), _p(kq), flags, _p(ids), _p(dis)))
         return ids, dis, off
 
     def capture_graph(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0):
+                      mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0, mixed_scan=False):
         """Capture a device-buffer search as a CUDA graph (see gbivf_graph_capture)."""
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
+        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
         g = C.c_void_p()
         check(self.lib.gbivf_graph_capture(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
                                            flags, C.c_void_p(d_ids_ptr), C.c_void_p(d_dis_ptr), C.c_void_p(d_w_ptr),

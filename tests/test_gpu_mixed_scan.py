@@ -1,0 +1,95 @@
+"""Precision form of the scan (GB300): FP16 approximate tables summed in FP32,
+then the alpha*k best re-scored in the reference's FP32 arithmetic. Every
+returned distance must be the plain form's for that id; ids match the plain
+form's except where a true neighbour fell outside the approximate selection."""
+import numpy as np
+import pytest
+
+from tests import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def compare(a_ids, a_dis, b_ids, b_dis):
+    """(fraction of identical rows, every matching id carries the same distance bits)."""
+    a_ids, b_ids = np.atleast_2d(a_ids), np.atleast_2d(b_ids)
+    a_dis, b_dis = np.atleast_2d(a_dis), np.atleast_2d(b_dis)
+    same_rows = np.mean([np.array_equal(x, y) for x, y in zip(a_ids, b_ids)])
+    ok = True
+    for ia, da, ib, db in zip(a_ids, a_dis, b_ids, b_dis):
+        pa = {int(i): float(d) for i, d in zip(ia, da) if i >= 0}
+        for i, d in zip(ib, db):
+            if i >= 0 and int(i) in pa and np.float32(pa[int(i)]).view(np.uint32) != np.float32(d).view(np.uint32):
+                ok = False
+    return same_rows, ok
+
+
+@pytest.mark.parametrize("name", ["cfg1", "m16"])
+@pytest.mark.parametrize("rerank", [False, True])
+def test_mixed_scan_golden(name, rerank):
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load(name)
+    gi = GpuIndex(g.ix, base=g.base)
+    w = g.meta["w"]
+    for k, kl in ((100, 100), (10, 100), (1, 50)):
+        a = gi.search(g.queries, k, w, kl=kl, rerank=rerank)
+        b = gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=True)
+        same, ok = compare(a[0], a[1], b[0], b[1])
+        print(f"[{name} rerank={rerank} k={k}] identical rows {same:.4f}")
+        assert ok, "a returned distance differs from the plain form's"
+        assert same >= 0.99
+    gi.close()
+
+
+def test_mixed_scan_uneven_batch_and_both_mixed_forms():
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load("m16")
+    rng = np.random.default_rng(9)
+    nq = len(g.queries)
+    wq = rng.integers(1, g.ix.coarsek + 1, nq).astype(np.int32)
+    kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
+    gi = GpuIndex(g.ix)
+    a_ids, a_dis, off = gi.search_batched(g.queries, wq, kq)
+    b_ids, b_dis, _ = gi.search_batched(g.queries, wq, kq, mixed_coarse=True, mixed_scan=True)
+    rows = [(a_ids[off[i]:off[i + 1]], a_dis[off[i]:off[i + 1]], b_ids[off[i]:off[i + 1]], b_dis[off[i]:off[i + 1]])
+            for i in range(nq)]
+    same = np.mean([np.array_equal(r[0], r[2]) for r in rows])
+    ok = all(compare(r[0], r[1], r[2], r[3])[1] for r in rows)
+    print(f"uneven: identical rows {same:.4f}")
+    assert ok and same >= 0.99
+    gi.close()
+
+
+def test_mixed_scan_on_gpu_built_zipf_index():
+    from mestrado_gb300.engine import GpuIndex
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
+    from mestrado_gb300.synth import Mixture
+
+    gm = GpuMixture(Mixture(d=128, ncomp=512, seed=13, zipf=1.1))
+    base = gm.generate(300000, stream_id=1)
+    train = gm.generate(60000, stream_id=2)
+    q = gm.generate(300, stream_id=3).cpu().numpy()
+    ix = build_index_gpu(base, train, coarsek=1024, m=16, niter=4, seed=2)
+    gi = GpuIndex(ix)
+    for k, w in ((100, 32), (1000, 64)):
+        a = gi.search(q, k, w)
+        b = gi.search(q, k, w, mixed_scan=True, mixed_coarse=True)
+        same, ok = compare(a[0], a[1], b[0], b[1])
+        recall = np.mean([len(set(x) & set(y)) / k for x, y in zip(a[0], b[0])])
+        print(f"k={k} w={w}: identical rows {same:.4f}, overlap with plain {recall:.5f}")
+        assert ok
+        assert recall >= 0.998
+    gi.close()
+
+
+def test_mixed_scan_rejects_direct_tables():
+    from mestrado_gb300.engine import GbivfError, GpuIndex
+
+    g = golden_cases.load("cfg1")
+    gi = GpuIndex(g.ix)
+    with pytest.raises(GbivfError) as e:
+        gi.search(g.queries, 10, 4, direct=True, mixed_scan=True)
+    assert e.value.code == 4
+    gi.close()
