@@ -41,9 +41,12 @@ __device__ __forceinline__ typename CodeRow<M>::T load_row(const uint8_t* p) {
     return __ldg(reinterpret_cast<const typename CodeRow<M>::T*>(p));
 }
 
+// byte s of v, zero-extended (one byte-permute)
+__device__ __forceinline__ uint32_t byte_of(uint32_t v, int s) { return __byte_perm(v, 0u, 0x4440u | (uint32_t)s); }
+
 __device__ __forceinline__ float adc4(float acc, uint32_t v, const float* T) {
 #pragma unroll
-    for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * 256 + ((v >> (8 * s)) & 0xff)]);
+    for (int s = 0; s < 4; s++) acc = __fadd_rn(acc, T[s * 256 + byte_of(v, s)]);
     return acc;
 }
 
@@ -66,7 +69,7 @@ __device__ __forceinline__ float add_f16(float acc, const __half* p) {
 }
 __device__ __forceinline__ float adc4h(float acc, uint32_t v, const __half* T) {
 #pragma unroll
-    for (int s = 0; s < 4; s++) acc = add_f16(acc, T + s * 256 + ((v >> (8 * s)) & 0xff));
+    for (int s = 0; s < 4; s++) acc = add_f16(acc, T + s * 256 + byte_of(v, s));
     return acc;
 }
 __device__ __forceinline__ float adc_sum16(uint32_t v, const __half* T) { return adc4h(0.0f, v, T) * 4.0f; }
@@ -110,10 +113,12 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     // this thread's slice of the codebook: sub-quantizer my_s, centroids
     // my_c0 .. my_c0+E-1 (consecutive, so the table row is one vector store)
     const int my_s = tid / TPS, my_c0 = (tid % TPS) * E;
-    float cen[E][DS];
-    float nhi[E], nlo[E];
+    // (the precision form builds its tables from per-list terms: no register codebook)
+    constexpr int EC = MIXED ? 1 : E;
+    float cen[EC][DS];
+    float nhi[EC], nlo[EC];
 #pragma unroll
-    for (int i = 0; i < E; i++) {
+    for (int i = 0; i < (MIXED ? 0 : E); i++) {
         const int e = my_s * KS + my_c0 + i;
         const float4* src = reinterpret_cast<const float4*>(ix.pq + (int64_t)e * DS);
 #pragma unroll
@@ -173,12 +178,51 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const float* xs = xq + my_s * DS;
 #pragma unroll
             for (int i = 0; i < E; i++) {
+                const float4* c4 = reinterpret_cast<const float4*>(ix.pq + (int64_t)(my_s * KS + my_c0 + i) * DS);
                 float dt = 0.0f;
 #pragma unroll
-                for (int t = 0; t < DS; t++) dt = __fmaf_rn(xs[t], cen[i][t], dt);
+                for (int v = 0; v < DS / 4; v++) {
+                    const float4 c = __ldg(c4 + v);
+                    dt = __fmaf_rn(xs[4 * v], c.x, dt);
+                    dt = __fmaf_rn(xs[4 * v + 1], c.y, dt);
+                    dt = __fmaf_rn(xs[4 * v + 2], c.z, dt);
+                    dt = __fmaf_rn(xs[4 * v + 3], c.w, dt);
+                }
                 q3[i] = -2.0f * dt;
             }
         }
+
+        // precision form: the next probe's table terms and first code chunk load during this probe
+        // (its table build is a few adds, too short to hide an HBM round trip)
+        CT pre[MIXED ? U : 1];
+        float t2n[MIXED ? E : 1];
+        auto load_probe = [&](int jj) {
+            if constexpr (MIXED) {
+                const int ll = jj < wq ? plist[jj] : -1;
+                const int ln = ll >= 0 ? __ldg(ix.list_len + ll) : 0;
+                const uint8_t* cp = ix.codes + (ll >= 0 ? __ldg(ix.list_beg + ll) : 0) * (int64_t)M;
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int i = u * NT + tid;
+                    pre[u] = i < ln ? load_row<M>(cp + (int64_t)i * M) : CT{};
+                }
+                const float* t2 = a.term2 + ((int64_t)(ll >= 0 ? ll : 0) * M + my_s) * KS + my_c0;
+                if constexpr (E % 4 == 0) {
+#pragma unroll
+                    for (int i = 0; i < E; i += 4) {
+                        const float4 v = ll >= 0 ? __ldg(reinterpret_cast<const float4*>(t2 + i)) : make_float4(0, 0, 0, 0);
+                        t2n[i] = v.x;
+                        t2n[i + 1] = v.y;
+                        t2n[i + 2] = v.z;
+                        t2n[i + 3] = v.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < E; i++) t2n[i] = ll >= 0 ? __ldg(t2 + i) : 0.0f;
+                }
+            }
+        };
+        load_probe(0);
 
         for (int j = 0; j < wq; j++) {
             const int jr = j % SP_RCH;
@@ -199,16 +243,26 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     for (int e = tid; e < nr * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
                 __syncthreads();
             }
+            CT cur[U];
+            float t2c[MIXED ? E : 1];
+            if constexpr (MIXED) {
+#pragma unroll
+                for (int u = 0; u < U; u++) cur[u] = pre[u];
+#pragma unroll
+                for (int i = 0; i < E; i++) t2c[i] = t2n[i];
+                load_probe(j + 1);
+            }
             const int l = plist[j];
             if (l < 0) continue;
             const int len = __ldg(ix.list_len + l);
             const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
-            // first chunk of codes in flight during the table build
-            CT cur[U];
+            if constexpr (!MIXED) {
+                // first chunk of codes in flight during the table build
 #pragma unroll
-            for (int u = 0; u < U; u++) {
-                const int i = u * NT + tid;
-                cur[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+                for (int u = 0; u < U; u++) {
+                    const int i = u * NT + tid;
+                    cur[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+                }
             }
             float* table = tables + (j & 1) * (M * KS);
             __half* table16 = reinterpret_cast<__half*>(tables) + (j & 1) * (M * KS);
@@ -216,10 +270,9 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                 // approximate entry ||r_s - c||^2 = term2[l][s][c] + q3 + ||r_s||^2, where
                 // term2 = ||c||^2 + 2 <y_{l,s}, c> is precomputed per list: 2 adds per entry
                 const float f = rn[jr * M + my_s];
-                const float* t2 = a.term2 + ((int64_t)l * M + my_s) * KS + my_c0;
                 unsigned short h[E];
 #pragma unroll
-                for (int i = 0; i < E; i++) h[i] = f16_sat((__ldg(t2 + i) + q3[i] + f) * SP_T16_SCALE);
+                for (int i = 0; i < E; i++) h[i] = f16_sat((t2c[i] + q3[i] + f) * SP_T16_SCALE);
                 __half* dst = table16 + my_s * KS + my_c0;
                 if constexpr (E == 8) {
                     *reinterpret_cast<uint4*>(dst) =
@@ -320,19 +373,21 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             u64 tk = *s.thresh;
             float td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
             uint32_t tp = key_payload(tk);
-            for (int i0 = 0; i0 < len; i0 += NT * U) {
-                CT nxt[U];
+            // two chunk buffers used in turn (unrolled by two, so nothing is copied between them)
+            auto load_chunk = [&](CT(&dst)[U], int i0) {
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int i = i0 + NT * U + u * NT + tid;
-                    nxt[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+                    const int i = i0 + u * NT + tid;
+                    dst[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
                 }
+            };
+            auto scan_chunk = [&](const CT(&c)[U], int i0) {
 #pragma unroll
                 for (int u = 0; u < U; u++) {
                     const int iw = i0 + u * NT + (tid & ~31);
                     if (iw < len) {
                         const int i = i0 + u * NT + tid;
-                        const float dist = MIXED ? adc_sum16(cur[u], table16) : adc_sum(cur[u], table);
+                        const float dist = MIXED ? adc_sum16(c[u], table16) : adc_sum(c[u], table);
                         const uint32_t pos = pos0 + (uint32_t)i;
                         const bool pass = i < len && (dist < td || (dist == td && pos < tp));
                         topk_push(s, make_key(dist, pos), pass);
@@ -344,8 +399,14 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
                     tp = key_payload(tk);
                 }
-#pragma unroll
-                for (int u = 0; u < U; u++) cur[u] = nxt[u];
+            };
+            for (int i0 = 0; i0 < len; i0 += 2 * NT * U) {
+                CT nxt[U];
+                load_chunk(nxt, i0 + NT * U);
+                scan_chunk(cur, i0);
+                if (i0 + NT * U >= len) break;
+                load_chunk(cur, i0 + 2 * NT * U);
+                scan_chunk(nxt, i0 + NT * U);
             }
         }
         // final merge; hand the unsorted best set (keys and base ids) over
@@ -603,12 +664,12 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
 template <int NT>
 static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
     const bool direct = a.flags & SCAN_TABLE_DIRECT;
-    if (a.flags & SCAN_MIXED) {  // the precision form: 512 threads, expansion tables
+    if (a.flags & SCAN_MIXED) {  // the precision form: expansion tables only
         if (direct) return cudaErrorNotSupported;
         switch (ix.m) {
-            case 4: return launch_sp<4, false, 512, true>(ix, a, num_sms, st);
-            case 8: return launch_sp<8, false, 512, true>(ix, a, num_sms, st);
-            default: return launch_sp<16, false, 512, true>(ix, a, num_sms, st);
+            case 4: return launch_sp<4, false, NT, true>(ix, a, num_sms, st);
+            case 8: return launch_sp<8, false, NT, true>(ix, a, num_sms, st);
+            default: return launch_sp<16, false, NT, true>(ix, a, num_sms, st);
         }
     }
     switch (ix.m) {
