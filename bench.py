@@ -50,6 +50,10 @@ CONFIGS = {
 # Larger workloads, generated and indexed on the GPU (gbivf_generate_mixture,
 # gbivf_kmeans, gbivf_pq_encode): the precision form against the plain one.
 LARGE = {
+    # the 100M workload's shape at 1/5 scale (20M base, 65,536 Zipf lists, m = 16, uneven nprobe / k):
+    # small enough to profile with every ncu section
+    "cfg4s": dict(d=128, ncomp=65536, seed=0, zipf=1.1, nbase=20_000_000, ntrain=655_360, nq=8192,
+                  C=65536, m=16, w=256, k=1000, uneven=True, train_iters=4, recall_q=256),
     # 10M base, 4,096-component mixture, 65,536 lists, m = 8, 10k queries, w = 32, k = 100
     "cfg3": dict(d=128, ncomp=4096, seed=0, zipf=None, nbase=10_000_000, ntrain=1_000_000, nq=10_000,
                  C=65536, m=8, w=32, k=100, uneven=False, train_iters=8, recall_q=1000),
@@ -416,8 +420,10 @@ def run_large(args, c, name, local_rank):
     # candidate bytes of the ADC scan: sum over queries of their probed lists' codes
     coa_idx, _ = gi.coarse_assign(queries.cpu().numpy(), max_w)
     scan_bytes = int(sum(sizes[coa_idx[i, :wq[i]]].sum() for i in range(nq))) * c["m"]
-    sample = min(nq, c["recall_q"])
-    gt = exact_topk(base, queries[:sample], max_k, batch=16 if c["nbase"] > 20_000_000 else 64)
+    sample = 0 if args.no_recall else min(nq, c["recall_q"])
+    gt = exact_topk(base, queries[:sample], max_k, batch=16 if c["nbase"] > 20_000_000 else 64) if sample else None
+    del base
+    torch.cuda.empty_cache()
 
     forms = {}
     for form, mixed in (("plain", False), ("mixed", True)):
@@ -450,7 +456,7 @@ def run_large(args, c, name, local_rank):
                                            C_ptr(d_dis), sp_ptr(sp))
         cm, sm = gi.last_stage_ms()
         rec = [len(set(ids[off[i]:off[i] + kq[i]].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i]
-               for i in range(sample)]
+               for i in range(sample)] or [float("nan")]
         forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps,
                            coarse_ms=cm, scan_ms=sm, recall=float(np.mean(rec)), clocks=clk, ids=ids,
                            dis=d_dis.cpu().numpy())
