@@ -52,6 +52,9 @@ extern "C" {
                                    plain form's and the ids match it unless a true neighbour fell outside
                                    the approximate selection */
 #define GBIVF_MIXED_SCAN_ALPHA 4
+#define GBIVF_RERANK_REFINE 0x20u /* re-rank the kl ADC candidates by the distance to their refined
+                                     reconstruction y + c1(codes) + c2(refinement codes) instead of the
+                                     raw vectors (needs gbivf_index_set_refine; k <= kl <= 1024) */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -83,6 +86,14 @@ int gbivf_index_create_from_lists(gbivf_index **out, int device, int d, int coar
                                   const float *const *pq_centroids, const int32_t *list_sizes,
                                   const int32_t *const *list_ids,
                                   const int32_t *const *list_codes);
+
+/* Refinement codes for GBIVF_RERANK_REFINE (no counterpart in the reference):
+ * a second product quantizer of the residual error e = x - y_list - c1(codes),
+ * m2 sub-quantizers of 256 centroids (pq2: m2 x 256 x 128/m2 floats, host),
+ * and one m2-byte code per indexed vector in the order of the index's ids
+ * (host codes2, or device d_codes2). d = 128. */
+int gbivf_index_set_refine(gbivf_index *ix, int m2, int ks2, const float *pq2, const uint8_t *codes2);
+int gbivf_index_set_refine_device(gbivf_index *ix, int m2, int ks2, const float *pq2, const uint8_t *d_codes2);
 
 /* Raw base vectors (n x d, row id = base id) for GBIVF_RERANK: the
  * `mat vbase` argument of ivfpq_search (sequential/ivf_pq/ivf_search.cpp:9,
@@ -255,6 +266,11 @@ int gbivf_assign(const float *d_x, int64_t n, int d, const float *d_centroids, i
  * residuals d_r (n x d); d_pq receives m x 256 x (d/m). */
 int gbivf_pq_train(const float *d_r, int64_t n, int d, int m, int niter, uint64_t seed, float *d_pq,
                    void *stream);
+
+/* The residual error a refinement quantizer encodes: d_out = x - coa[coarse]
+ * - c1(codes), n x d (d_coarse may be NULL). Device buffers; synchronous. */
+int gbivf_pq_error(const float *d_x, int64_t n, int d, const int32_t *d_coarse, const float *d_coa, int m,
+                   const float *d_pq, const uint8_t *d_codes, float *d_out, void *stream);
 
 /* PQ codes (n x m bytes) of rows d_x, of their residuals to d_coa[d_coarse[i]]
  * when d_coarse is not NULL. */

@@ -107,6 +107,8 @@ struct gbivf_index {
     int device = 0;
     DevIndex dx;
     std::vector<int32_t> h_len;  // list sizes (host copy)
+    std::vector<int64_t> h_off, h_beg;  // list offsets in the caller's (unpadded) order, padded first rows
+    DBuf pq2, codes2;            // refinement codebook and codes (gbivf_index_set_refine)
     int32_t min_id = 0, max_id = -1;  // range of stored base ids (re-rank bounds)
     int num_sms = 0;
     bool mixed_pending = false;       // a coarse stage with device flags ran since the last flag check
@@ -150,7 +152,8 @@ void free_index(gbivf_index* ix) {
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
-                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->term2, &ix->w_clist})
+                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->term2, &ix->w_clist,
+                    &ix->pq2, &ix->codes2})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -196,6 +199,7 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     const int64_t align_rows = 16 / g16;
     std::vector<int64_t> beg(coarsek);
     ix->h_len.resize(coarsek);
+    ix->h_off.assign(list_off, list_off + coarsek + 1);
     int64_t rows = 0;
     for (int l = 0; l < coarsek; l++) {
         rows = (rows + align_rows - 1) / align_rows * align_rows;
@@ -204,6 +208,7 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         rows += ix->h_len[l];
     }
     rows = (rows + align_rows - 1) / align_rows * align_rows;
+    ix->h_beg = beg;
     std::vector<uint8_t> pcodes((size_t)std::max<int64_t>(rows, 1) * nsq, 0);
     std::vector<int32_t> pids((size_t)std::max<int64_t>(rows, 1), -1);
     for (int l = 0; l < coarsek; l++) {
@@ -293,7 +298,10 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
             return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN needs d = 128, ks = 256, m in {4, 8, 16} and "
                                                "k (or kl) <= 1024");
     }
-    if (mixed || (ix->use_persistent && scan_persistent_supported(ix->dx, a))) {
+    const bool refine = a.flags & SCAN_REFINE;
+    if (refine && !scan_persistent_supported(ix->dx, a))
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_RERANK_REFINE needs d = 128, ks = 256, m in {4, 8, 16}");
+    if (mixed || refine || (ix->use_persistent && scan_persistent_supported(ix->dx, a))) {
         const int stride = scan_persistent_stride(a);
         CK(ix->w_ckey.ensure(sizeof(unsigned long long) * (size_t)a.nq * stride));
         CK(ix->w_cid.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
@@ -302,7 +310,7 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
         a.cand_id = ix->w_cid.as<int32_t>();
         a.cand_cnt = ix->w_ccnt.as<int32_t>();
         a.cand_stride = stride;
-        if (mixed) {
+        if (mixed || refine) {
             CK(ix->w_clist.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
             a.cand_list = ix->w_clist.as<int32_t>();
         }
@@ -320,10 +328,17 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
     if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL |
-                  GBIVF_MIXED_SCAN))
+                  GBIVF_MIXED_SCAN | GBIVF_RERANK_REFINE))
         return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
     if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_TABLE_DIRECT))
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN uses the expansion tables (not GBIVF_TABLE_DIRECT)");
+    if (flags & GBIVF_RERANK_REFINE) {
+        if (flags & (GBIVF_RERANK | GBIVF_TABLE_DIRECT))
+            return fail(GBIVF_ERR_INVALID, "GBIVF_RERANK_REFINE excludes GBIVF_RERANK and GBIVF_TABLE_DIRECT");
+        if (!ix->dx.codes2) return fail(GBIVF_ERR_INVALID, "GBIVF_RERANK_REFINE needs gbivf_index_set_refine first");
+        if (kl <= 0 || kl > 1024 || kl < k)
+            return fail(GBIVF_ERR_UNSUPPORTED, "kl=%d: the refinement re-rank takes k <= kl <= 1024", kl);
+    }
     if ((flags & GBIVF_MIXED_COARSE) && ix->dx.d != 128)
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_COARSE needs d = 128 (d = %d)", ix->dx.d);
     if (flags & GBIVF_RERANK) {
@@ -566,7 +581,7 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.k = k;
     a.kl = kl;
     a.flags = (flags & GBIVF_RERANK ? SCAN_RERANK : 0) | (flags & GBIVF_TABLE_DIRECT ? SCAN_TABLE_DIRECT : 0) |
-              (flags & GBIVF_MIXED_SCAN ? SCAN_MIXED : 0);
+              (flags & GBIVF_MIXED_SCAN ? SCAN_MIXED : 0) | (flags & GBIVF_RERANK_REFINE ? SCAN_REFINE : 0);
     a.queries = d_q;
     a.qnorm = qn;
     a.probes = coaidx;
@@ -647,6 +662,63 @@ int gbivf_index_set_base(gbivf_index* ix, const float* base, int64_t n, int d) {
     ix->dx.base_norm = ix->base_norm.as<float>();
     ix->dx.nbase = n;
     return GBIVF_OK;
+}
+
+// refinement codes: codebook m2 x 256 x (d/m2) floats (host), codes n x m2 bytes in the caller's
+// list order (host or device), placed in the padded row layout of the PQ codes
+static int set_refine_impl(gbivf_index* ix, int m2, int ks2, const float* pq2, const uint8_t* codes2, bool on_device) {
+    if (!ix || !pq2 || (!codes2 && ix->h_off.back() > 0)) return fail(GBIVF_ERR_INVALID, "bad refinement arguments");
+    const DevIndex& dx = ix->dx;
+    if (dx.d != 128) return fail(GBIVF_ERR_UNSUPPORTED, "refinement codes need d = 128 (d = %d)", dx.d);
+    if (ks2 != 256) return fail(GBIVF_ERR_UNSUPPORTED, "refinement codebooks have 256 centroids (ks2 = %d)", ks2);
+    if (m2 <= 0 || 128 % m2 || (128 / m2) % 4) return fail(GBIVF_ERR_UNSUPPORTED, "m2 = %d (a divisor of 32)", m2);
+    if ((dx.ds % 4) != 0) return fail(GBIVF_ERR_UNSUPPORTED, "refinement re-rank needs d/m a multiple of 4");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    DeviceGuard g(ix->device);
+    const int64_t n = ix->h_off.back(), rows = dx.rows;
+    CK(ix->pq2.ensure(sizeof(float) * 256 * 128));
+    CK(cudaMemcpyAsync(ix->pq2.p, pq2, sizeof(float) * 256 * 128, cudaMemcpyHostToDevice, ix->stream));
+    CK(ix->codes2.ensure((size_t)std::max<int64_t>(rows, 1) * m2));
+    CK(cudaMemsetAsync(ix->codes2.p, 0, (size_t)std::max<int64_t>(rows, 1) * m2, ix->stream));
+    if (n > 0) {
+        if (on_device) {
+            DBuf off, beg;
+            CK(off.ensure(sizeof(int64_t) * ix->h_off.size()));
+            CK(beg.ensure(sizeof(int64_t) * ix->h_beg.size()));
+            CK(cudaMemcpyAsync(off.p, ix->h_off.data(), sizeof(int64_t) * ix->h_off.size(), cudaMemcpyHostToDevice,
+                               ix->stream));
+            CK(cudaMemcpyAsync(beg.p, ix->h_beg.data(), sizeof(int64_t) * ix->h_beg.size(), cudaMemcpyHostToDevice,
+                               ix->stream));
+            CK(launch_scatter_rows(codes2, off.as<int64_t>(), beg.as<int64_t>(), dx.C, m2, ix->codes2.as<uint8_t>(),
+                                   ix->stream));
+            CK(cudaStreamSynchronize(ix->stream));
+            off.release();
+            beg.release();
+        } else {
+            std::vector<uint8_t> pc((size_t)rows * m2, 0);
+            for (int l = 0; l < dx.C; l++) {
+                const int64_t len = ix->h_off[l + 1] - ix->h_off[l];
+                if (len) memcpy(&pc[(size_t)ix->h_beg[l] * m2], codes2 + ix->h_off[l] * m2, (size_t)len * m2);
+            }
+            CK(cudaMemcpyAsync(ix->codes2.p, pc.data(), pc.size(), cudaMemcpyHostToDevice, ix->stream));
+            CK(cudaStreamSynchronize(ix->stream));
+        }
+    } else {
+        CK(cudaStreamSynchronize(ix->stream));
+    }
+    ix->dx.m2 = m2;
+    ix->dx.ds2 = 128 / m2;
+    ix->dx.pq2 = ix->pq2.as<float>();
+    ix->dx.codes2 = ix->codes2.as<uint8_t>();
+    return GBIVF_OK;
+}
+
+int gbivf_index_set_refine(gbivf_index* ix, int m2, int ks2, const float* pq2, const uint8_t* codes2) {
+    return set_refine_impl(ix, m2, ks2, pq2, codes2, false);
+}
+
+int gbivf_index_set_refine_device(gbivf_index* ix, int m2, int ks2, const float* pq2, const uint8_t* d_codes2) {
+    return set_refine_impl(ix, m2, ks2, pq2, d_codes2, true);
 }
 
 int gbivf_index_destroy(gbivf_index* ix) {
@@ -915,7 +987,7 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
 int gbivf_search_batched_device(gbivf_index* ix, const float* d_queries, int nq, const int32_t* d_w,
                                 const int32_t* d_k, const int64_t* d_out_off, int max_w, int max_k, unsigned flags,
                                 int32_t* d_ids, float* d_dis, void* stream) {
-    if (flags & GBIVF_RERANK) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
+    if (flags & (GBIVF_RERANK | GBIVF_RERANK_REFINE)) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
     int rc = check_search(ix, nq, max_k, max_k, max_w, flags);
     if (rc) return rc;
     if (nq > 0 && (!d_queries || !d_w || !d_k || !d_out_off || !d_ids || !d_dis))
@@ -932,7 +1004,7 @@ int gbivf_search_batched(gbivf_index* ix, const float* queries, int nq, const in
     if (nq < 0) return fail(GBIVF_ERR_INVALID, "nq=%d", nq);
     if (nq == 0) return GBIVF_OK;
     if (!queries || !w_per_q || !k_per_q || !ids || !dis) return fail(GBIVF_ERR_INVALID, "NULL host buffer");
-    if (flags & GBIVF_RERANK) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
+    if (flags & (GBIVF_RERANK | GBIVF_RERANK_REFINE)) return fail(GBIVF_ERR_UNSUPPORTED, "uneven batches do not re-rank");
     int max_w = 0, max_k = 0;
     std::vector<int64_t> off(nq);
     int64_t total = 0;
@@ -1229,6 +1301,15 @@ int gbivf_pq_train(const float* d_r, int64_t n, int d, int m, int niter, uint64_
     const int ds = d / m;
     if (ds != 8 && ds != 16 && ds != 32) return fail(GBIVF_ERR_UNSUPPORTED, "sub-vector length %d (8, 16, 32)", ds);
     CK(pq_train_rows(d_r, n, d, m, niter, seed, d_pq, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_pq_error(const float* d_x, int64_t n, int d, const int32_t* d_coarse, const float* d_coa, int m,
+                   const float* d_pq, const uint8_t* d_codes, float* d_out, void* stream) {
+    if (!d_x || !d_pq || !d_codes || !d_out || n < 0 || m <= 0 || d % m || (d_coarse && !d_coa))
+        return fail(GBIVF_ERR_INVALID, "bad PQ error arguments");
+    CK(pq_error_rows(d_x, n, d, d_coarse, d_coa, m, d_pq, d_codes, d_out, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
     return GBIVF_OK;
 }
 

@@ -186,6 +186,18 @@ __global__ void residual_kernel(const float* __restrict__ x, int64_t n, int d, c
     r[t] = x[t] - coa[(int64_t)assign[i] * d + l];
 }
 
+// e = x - coa[assign] - c1(codes): the residual error a refinement quantizer encodes
+__global__ void pq_error_kernel(const float* __restrict__ x, int64_t n, int d, const int32_t* __restrict__ assign,
+                                const float* __restrict__ coa, int m, const float* __restrict__ pq,
+                                const uint8_t* __restrict__ codes, float* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * d) return;
+    const int64_t i = t / d;
+    const int l = (int)(t % d), ds = d / m, s = l / ds;
+    const float y = assign ? coa[(int64_t)assign[i] * d + l] : 0.0f;
+    out[t] = x[t] - y - pq[((int64_t)s * 256 + codes[i * m + s]) * ds + (l - s * ds)];
+}
+
 __global__ void store_codes_kernel(const int32_t* __restrict__ a, int64_t n, int m, int s, uint8_t* __restrict__ codes) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) codes[i * m + s] = (uint8_t)a[i];
@@ -333,6 +345,13 @@ cudaError_t pq_encode_rows(const float* x, int64_t n, int d, const int32_t* coar
     cudaFree(res);
     cudaFree(a);
     return e;
+}
+
+cudaError_t pq_error_rows(const float* x, int64_t n, int d, const int32_t* coarse, const float* coa, int m,
+                          const float* pq, const uint8_t* codes, float* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    pq_error_kernel<<<blocks(n * d, 256), 256, 0, st>>>(x, n, d, coarse, coa, m, pq, codes, out);
+    return cudaGetLastError();
 }
 
 }  // namespace gbivf

@@ -136,6 +136,23 @@ cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const 
     return cudaGetLastError();
 }
 
+// one CTA per list: copy its rows from the caller's order into the padded row layout
+__global__ void scatter_rows_kernel(const uint8_t* __restrict__ src, const int64_t* __restrict__ off,
+                                    const int64_t* __restrict__ beg, int width, uint8_t* __restrict__ dst) {
+    const int l = blockIdx.x;
+    const int64_t n = (off[l + 1] - off[l]) * width;
+    const uint8_t* s = src + off[l] * width;
+    uint8_t* d = dst + beg[l] * width;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+}
+
+cudaError_t launch_scatter_rows(const uint8_t* src, const int64_t* off, const int64_t* beg, int C, int width,
+                                uint8_t* dst, cudaStream_t st) {
+    if (C <= 0) return cudaSuccess;
+    scatter_rows_kernel<<<C, 256, 0, st>>>(src, off, beg, width, dst);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // precision form of the scan: per-list table terms
 // ||r_s - c||^2 = ||r_s||^2 - 2 <x_s, c> + (||c||^2 + 2 <y_{l,s}, c>), r = x - y_l;

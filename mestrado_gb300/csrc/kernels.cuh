@@ -12,6 +12,7 @@ enum ScanFlags : int {
     SCAN_SRC_RESIDUAL = 4,  // residuals are given (nq*w x d) instead of queries
     SCAN_OUT_PACKED = 8,    // write min(L, k) results at out_start[q] (core_gpu)
     SCAN_MIXED = 16,        // precision form: FP16 approximate tables, exact re-score of alpha*k
+    SCAN_REFINE = 32,       // re-rank the kl ADC candidates by their refined reconstruction
 };
 
 // Device view of one index (all pointers in device memory).
@@ -31,6 +32,11 @@ struct DevIndex {
     const float* base = nullptr;       // nbase x d raw vectors (re-rank)
     const float* base_norm = nullptr;  // nbase float norms
     int64_t nbase = 0;
+    // refinement codes of the residual error (x - y_l - c1(codes)): m2 x 256 x ds2 codebook,
+    // rows x m2 codes in the row layout of `codes`
+    int m2 = 0, ds2 = 0;
+    const float* pq2 = nullptr;
+    const uint8_t* codes2 = nullptr;
 };
 
 struct ScanArgs {
@@ -94,6 +100,10 @@ cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int nu
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
+
+// rows of `width` bytes in list order (list l: rows off[l] .. off[l+1]) -> dst rows beg[l] ..
+cudaError_t launch_scatter_rows(const uint8_t* src, const int64_t* off, const int64_t* beg, int C, int width,
+                                uint8_t* dst, cudaStream_t st);
 
 // precision form of the scan: term2[l][s][c] = ||c||^2 + 2 <y_{l,s}, c> for every list (C x m x ks)
 cudaError_t launch_term2(const DevIndex& ix, float* term2, cudaStream_t st);
@@ -199,6 +209,9 @@ cudaError_t pq_train_rows(const float* r, int64_t n, int d, int m, int niter, ui
                           cudaStream_t st);
 cudaError_t pq_encode_rows(const float* x, int64_t n, int d, const int32_t* coarse, const float* coa, int m,
                            const float* pq, uint8_t* codes, cudaStream_t st);
+// out = x - coa[coarse] - c1(codes) (coarse may be NULL), n x d
+cudaError_t pq_error_rows(const float* x, int64_t n, int d, const int32_t* coarse, const float* coa, int m,
+                          const float* pq, const uint8_t* codes, float* out, cudaStream_t st);
 
 // largest k / kl / w the scan kernel supports
 constexpr int MAX_K = 2048;

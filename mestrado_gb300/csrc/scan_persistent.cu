@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
 
     const int tid = threadIdx.x, lane = tid & 31, w = a.w;  // w: the probes row stride
     const bool src_res = a.flags & SCAN_SRC_RESIDUAL;
+    const bool rows_out = MIXED || (a.flags & SCAN_REFINE);  // hand off code rows and lists
 
     // this thread's slice of the codebook: sub-quantizer my_s, centroids
     // my_c0 .. my_c0+E-1 (consecutive, so the table row is one vector store)
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
         if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
         // this query's probe count and result count (uneven batches)
         const int wq = query_w(a, q);
-        const int kq0 = (a.flags & SCAN_RERANK) ? a.kl : query_k(a, q);
+        const int kq0 = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : query_k(a, q);
         // the precision form keeps alpha * k approximate candidates for the exact re-score
         const int kq = MIXED ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
         if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
@@ -421,8 +422,8 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const int64_t o = (int64_t)q * a.cand_stride + c;
             if (c < nbest) {
                 a.cand_key[o] = best[c];
-                if constexpr (MIXED) {
-                    // the code row and its list, for the exact re-score
+                if (rows_out) {
+                    // the code row and its list, for the exact re-score or the refinement re-rank
                     const uint32_t pos = key_payload(best[c]);
                     const int jj = probe_of(prefix, wq, pos);
                     const int ll = plist[jj];
@@ -434,7 +435,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             } else {
                 a.cand_key[o] = KEY_MAX;
                 a.cand_id[o] = -1;
-                if constexpr (MIXED) a.cand_list[o] = 0;
+                if (rows_out) a.cand_list[o] = 0;
             }
         }
         if (tid == 0) a.cand_cnt[q] = nbest;
@@ -526,6 +527,35 @@ __device__ __forceinline__ float exact_adc(const DevIndex& ix, const float* xq, 
     return dist;
 }
 
+// Distance from the query to the refined reconstruction y_l + c1(codes) + c2(codes2) of one code
+// row (refinement codes of the residual error), FP32 in dimension order. d = 128.
+__device__ inline float refined_dist(const DevIndex& ix, const float* xq, int l, int64_t row) {
+    const int m = ix.m, ds = ix.ds, m2 = ix.m2, ds2 = ix.ds2;
+    const uint8_t* c1 = ix.codes + row * m;
+    const uint8_t* c2 = ix.codes2 + row * m2;
+    const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128);
+    float dist = 0.0f;
+#pragma unroll 4
+    for (int t4 = 0; t4 < 32; t4++) {
+        const int t = 4 * t4, s = t / ds, s2 = t / ds2;
+        const float4 y = __ldg(y4 + t4);
+        const float4 a = __ldg(reinterpret_cast<const float4*>(ix.pq + ((int64_t)s * 256 + c1[s]) * ds + (t - s * ds)));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(ix.pq2 + ((int64_t)s2 * 256 + c2[s2]) * ds2 + (t - s2 * ds2)));
+        const float e0 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t], y.x), a.x), b.x);
+        const float e1 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 1], y.y), a.y), b.y);
+        const float e2 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 2], y.z), a.z), b.z);
+        const float e3 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 3], y.w), a.w), b.w);
+        dist = __fadd_rn(dist, __fmul_rn(e0, e0));
+        dist = __fadd_rn(dist, __fmul_rn(e1, e1));
+        dist = __fadd_rn(dist, __fmul_rn(e2, e2));
+        dist = __fadd_rn(dist, __fmul_rn(e3, e3));
+    }
+    return dist;
+}
+
+// Per query (one CTA): order the hand-off set, then write it, or re-rank it and write the k best.
+// The sort carries the keys and, with them, either base ids (the exact form) or hand-off slots
+// (precision form, refinement re-rank: the slot leads to the candidate's code row and list).
 template <bool MIXED, int M = 8>
 __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
@@ -534,17 +564,19 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
     float* xq = reinterpret_cast<float*>(ids + n2);
     const int q = blockIdx.x, tid = threadIdx.x;
+    const bool rerank = a.flags & SCAN_RERANK, refine = a.flags & SCAN_REFINE;
+    const bool slots = MIXED || refine;  // ids[] holds hand-off slots, not base ids
+    const int64_t hb = (int64_t)q * n2;  // this query's hand-off slots
     int n = a.cand_cnt[q];
     // only this query's candidates are sorted: the smallest power of two holding them (the
     // hand-off pads with KEY_MAX), not the batch-wide stride
     int p2 = 2;
     while (p2 < n) p2 <<= 1;
     for (int c = tid; c < p2; c += FIN_NT) {
-        keys[c] = a.cand_key[(int64_t)q * n2 + c];
-        ids[c] = a.cand_id[(int64_t)q * n2 + c];
+        keys[c] = a.cand_key[hb + c];
+        ids[c] = slots ? c : a.cand_id[hb + c];
     }
-    const bool rerank = a.flags & SCAN_RERANK;
-    if (rerank || MIXED)
+    if (rerank || slots)
         for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
     __syncthreads();
     if constexpr (MIXED) {
@@ -554,38 +586,38 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
         for (int c = tid; c < p2; c += FIN_NT) {
             u64 key = KEY_MAX;
             if (c < n) {
-                const float dist = exact_adc<M>(ix, xq, a.cand_list[(int64_t)q * n2 + c], ids[c]);
+                const float dist = exact_adc<M>(ix, xq, a.cand_list[hb + c], a.cand_id[hb + c]);
                 key = make_key(dist, key_payload(keys[c]));
             }
             keys[c] = key;
         }
         __syncthreads();
         bitonic_sort_pairs(keys, ids, p2);
-        for (int c = tid; c < n; c += FIN_NT) ids[c] = ix.ids[ids[c]];  // code rows -> base ids
-        __syncthreads();
-        n = min(n, rerank ? a.kl : query_k(a, q));
+        n = min(n, (rerank || refine) ? a.kl : query_k(a, q));
     } else {
         bitonic_sort_pairs(keys, ids, p2);
     }
+    auto base_id = [&](int c) { return slots ? ix.ids[a.cand_id[hb + ids[c]]] : ids[c]; };
     const float inf = __int_as_float(0x7f800000);
-    if (!rerank) {
+    if (!rerank && !refine) {
         if (a.flags & SCAN_OUT_PACKED) {
             const int64_t o = a.out_start[q];
             for (int c = tid; c < n; c += FIN_NT) {
-                a.out_ids[o + c] = ids[c];
+                a.out_ids[o + c] = base_id(c);
                 a.out_dis[o + c] = key_dist(keys[c]);
             }
         } else {
             const int kq = query_k(a, q);
             const int64_t o = query_out(a, q);
             for (int c = tid; c < kq; c += FIN_NT) {
-                a.out_ids[o + c] = c < n ? ids[c] : -1;
+                a.out_ids[o + c] = c < n ? base_id(c) : -1;
                 a.out_dis[o + c] = c < n ? key_dist(keys[c]) : inf;
             }
         }
         return;
     }
-    // exact distances of the n candidates in ADC order, keyed by that rank
+    // re-rank the n candidates in ADC order: exact L2 to the raw vector (ivf_search.cpp:113-134)
+    // or the refined distance, keyed by the ADC rank
     const double qn = a.qnorm[q];
     const int d = ix.d;
     int pr = 2;
@@ -593,18 +625,26 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     for (int c = tid; c < pr; c += FIN_NT) {
         u64 key = KEY_MAX;
         if (c < n) {
-            const float4* v4 = reinterpret_cast<const float4*>(ix.base + (int64_t)ids[c] * d);
-            float dot = 0.0f;
-            for (int l = 0; l < d / 4; l++) {
-                const float4 b = __ldg(v4 + l);
-                dot = __fadd_rn(dot, __fmul_rn(b.x, xq[4 * l]));
-                dot = __fadd_rn(dot, __fmul_rn(b.y, xq[4 * l + 1]));
-                dot = __fadd_rn(dot, __fmul_rn(b.z, xq[4 * l + 2]));
-                dot = __fadd_rn(dot, __fmul_rn(b.w, xq[4 * l + 3]));
+            float dist;
+            if (refine) {
+                const int64_t slot = hb + ids[c];
+                dist = refined_dist(ix, xq, a.cand_list[slot], a.cand_id[slot]);
+            } else {
+                const int32_t id = base_id(c);
+                const float4* v4 = reinterpret_cast<const float4*>(ix.base + (int64_t)id * d);
+                float dot = 0.0f;
+                for (int l = 0; l < d / 4; l++) {
+                    const float4 b = __ldg(v4 + l);
+                    dot = __fadd_rn(dot, __fmul_rn(b.x, xq[4 * l]));
+                    dot = __fadd_rn(dot, __fmul_rn(b.y, xq[4 * l + 1]));
+                    dot = __fadd_rn(dot, __fmul_rn(b.z, xq[4 * l + 2]));
+                    dot = __fadd_rn(dot, __fmul_rn(b.w, xq[4 * l + 3]));
+                }
+                dist = expansion_from(qn, ix.base_norm[id], dot);
             }
-            key = make_key(expansion_from(qn, ix.base_norm[ids[c]], dot), (uint32_t)c);
+            key = make_key(dist, (uint32_t)c);
         }
-        keys[c] = key;
+        keys[c] = key;  // (ids[] keeps the ADC order the payload refers to)
     }
     __syncthreads();
     bitonic_sort_smem(keys, pr);
@@ -612,22 +652,25 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     const int64_t o = query_out(a, q);
     const int kr = min(kq, n);
     for (int c = tid; c < kq; c += FIN_NT) {
-        a.out_ids[o + c] = c < kr ? ids[key_payload(keys[c])] : -1;
+        a.out_ids[o + c] = c < kr ? base_id(key_payload(keys[c])) : -1;
         a.out_dis[o + c] = c < kr ? key_dist(keys[c]) : inf;
     }
 }
 
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
-    const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
+    const int kk = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : a.k;
     const bool m_ok = ix.m == 4 || ix.m == 8 || ix.m == 16;
     const bool mixed_ok = !(a.flags & SCAN_MIXED) ||
                           !(a.flags & (SCAN_TABLE_DIRECT | SCAN_SRC_RESIDUAL | SCAN_OUT_PACKED));
+    const bool refine_ok = !(a.flags & SCAN_REFINE) ||
+                           !(a.flags & (SCAN_RERANK | SCAN_SRC_RESIDUAL | SCAN_OUT_PACKED));
     return ix.d == 128 && ix.ks == 256 && m_ok && std::max(kk, a.k) <= 1024 && a.queue != nullptr &&
-           ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK)) && mixed_ok;
+           ix.pq_hi != nullptr && !((a.flags & SCAN_SRC_RESIDUAL) && (a.flags & SCAN_RERANK)) && mixed_ok &&
+           refine_ok;
 }
 
 int scan_persistent_stride(const ScanArgs& a) {
-    const int kk = (a.flags & SCAN_RERANK) ? a.kl : a.k;
+    const int kk = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : a.k;
     const int sel = (a.flags & SCAN_MIXED) ? std::min(kk * a.sel_mult, a.sel_cap) : kk;
     return pow2_at_least(std::max(std::max(sel, a.k), 2));
 }
@@ -637,6 +680,7 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
     const int kcap = scan_persistent_stride(a);
     if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
     if (MIXED && (!a.term2 || !a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
+    if ((a.flags & SCAN_REFINE) && (!a.cand_list || !ix.codes2 || !ix.pq2)) return cudaErrorInvalidValue;
     ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH);
     auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT, MIXED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);

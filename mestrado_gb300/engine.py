@@ -46,6 +46,9 @@ class GpuIndex:
                                           data.ks, _p(keep[1]), _p(keep[2]), _p(keep[3]), _p(keep[4])))
         self.h = h
         self.base_rows = 0
+        if data.pq2 is not None:
+            p2, c2 = _c(data.pq2, np.float32), _c(data.codes2, np.uint8)
+            check(self.lib.gbivf_index_set_refine(h, data.pq2.shape[0], 256, _p(p2), _p(c2)))
         if base is not None:
             self.set_base(base)
 
@@ -82,7 +85,7 @@ class GpuIndex:
 
     # -- searches ---------------------------------------------------------
     def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False,
-               mixed_scan=False):
+               mixed_scan=False, refine=False):
         """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
         pass preallocated (ids, dis) host arrays (e.g. pinned memory)."""
         q = _c(queries, np.float32)
@@ -97,16 +100,18 @@ class GpuIndex:
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
         return ids, dis
 
     def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False):
+                      stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False, refine=False):
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
@@ -126,10 +131,12 @@ class GpuIndex:
         return ids, dis, off
 
     def capture_graph(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0, mixed_scan=False):
+                      mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0, mixed_scan=False,
+                      refine=False):
         """Capture a device-buffer search as a CUDA graph (see gbivf_graph_capture)."""
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
         flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         g = C.c_void_p()
         check(self.lib.gbivf_graph_capture(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
                                            flags, C.c_void_p(d_ids_ptr), C.c_void_p(d_dis_ptr), C.c_void_p(d_w_ptr),

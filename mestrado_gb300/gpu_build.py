@@ -10,7 +10,9 @@ this driver runs every step on the GPU:
 4. base vectors: nearest coarse centroid (gbivf_assign), PQ codes of the
    residuals (gbivf_pq_encode);
 5. lists bucketed by coarse centroid with ids ascending (stable sort on the
-   host, as the reference's ivec_sort_index orders them).
+   host, as the reference's ivec_sort_index orders them);
+6. optionally, refinement codes: a second product quantizer trained on and
+   encoding the residual errors x - y_list - c1(codes) (gbivf_pq_error).
 
 Device buffers are torch tensors (memory only); all compute is the engine's.
 """
@@ -100,19 +102,71 @@ def encode_base(base, coa, pq, chunk: int = 1 << 24):
     return assign, codes
 
 
-def bucket(assign: np.ndarray, codes: np.ndarray, coarsek: int):
+def residual_error(x, assign, coa, pq, codes):
+    """x - coa[assign] - c1(codes) on the GPU (the refinement quantizer's input)."""
+    import torch
+
+    lib = _lib.load()
+    n, d = x.shape
+    out = torch.empty_like(x)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    check(lib.gbivf_pq_error(_ptr(x), n, d, _ptr(assign), _ptr(coa), pq.shape[0], _ptr(pq), _ptr(codes), _ptr(out), s))
+    return out
+
+
+def train_refine(train, coa, pq, m2: int, niter: int = 10, seed: int = 0):
+    """Refinement codebook (m2 x 256 x d/m2) trained on the residual errors of
+    the training set (a second product quantizer; no counterpart in the reference)."""
+    import torch
+
+    lib = _lib.load()
+    assign, codes = encode_base(train, coa, pq)
+    err = residual_error(train, assign, coa, pq, codes)
+    n, d = train.shape
+    pq2 = torch.empty((m2, 256, d // m2), dtype=torch.float32, device=train.device)
+    check(lib.gbivf_pq_train(_ptr(err), n, d, m2, niter, seed + 7, _ptr(pq2),
+                             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return pq2
+
+
+def encode_refine(base, assign, codes, coa, pq, pq2, chunk: int = 1 << 22):
+    """Refinement codes of the base set (n x m2 uint8, device)."""
+    import torch
+
+    lib = _lib.load()
+    n, d = base.shape
+    m2 = pq2.shape[0]
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    codes2 = torch.empty((n, m2), dtype=torch.uint8, device=base.device)
+    for r in range(0, n, chunk):
+        nb = min(chunk, n - r)
+        err = residual_error(base[r:r + nb], assign[r:r + nb], coa, pq, codes[r:r + nb])
+        check(lib.gbivf_pq_encode(_ptr(err), nb, d, C.c_void_p(0), C.c_void_p(0), m2, _ptr(pq2),
+                                  _ptr(codes2[r:r + nb]), s))
+    return codes2
+
+
+def bucket(assign: np.ndarray, codes: np.ndarray, coarsek: int, codes2: np.ndarray | None = None):
     order = np.argsort(assign, kind="stable")
     counts = np.bincount(assign, minlength=coarsek)
     off = np.zeros(coarsek + 1, np.int64)
     np.cumsum(counts, out=off[1:])
-    return off, order.astype(np.int32), np.ascontiguousarray(codes[order])
+    c2 = None if codes2 is None else np.ascontiguousarray(codes2[order])
+    return off, order.astype(np.int32), np.ascontiguousarray(codes[order]), c2
 
 
-def build_index_gpu(base, train, coarsek: int, m: int, niter: int = 10, seed: int = 0) -> IVFPQData:
+def build_index_gpu(base, train, coarsek: int, m: int, niter: int = 10, seed: int = 0, m2: int = 0) -> IVFPQData:
+    """An index built on the GPU; with m2 > 0 also m2 x 256 refinement codes."""
     coa, pq = train_quantizers(train, coarsek, m, niter, seed)
     assign, codes = encode_base(base, coa, pq)
-    off, ids, codes_h = bucket(assign.cpu().numpy(), codes.cpu().numpy(), coarsek)
-    out = IVFPQData(coa=coa.cpu().numpy(), pq=pq.cpu().numpy(), list_off=off, ids=ids, codes=codes_h)
+    pq2 = codes2 = None
+    if m2:
+        pq2 = train_refine(train, coa, pq, m2, niter, seed)
+        codes2 = encode_refine(base, assign, codes, coa, pq, pq2)
+    off, ids, codes_h, codes2_h = bucket(assign.cpu().numpy(), codes.cpu().numpy(), coarsek,
+                                         None if codes2 is None else codes2.cpu().numpy())
+    out = IVFPQData(coa=coa.cpu().numpy(), pq=pq.cpu().numpy(), list_off=off, ids=ids, codes=codes_h,
+                    pq2=None if pq2 is None else pq2.cpu().numpy(), codes2=codes2_h)
     out.validate()
     return out
 

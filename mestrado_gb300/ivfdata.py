@@ -11,6 +11,9 @@ plus an ``ivfpq_t`` with the coarse centroids and a ``pqtipo`` holding
 * ``list_off`` C+1 int64 offsets; list l is rows ``list_off[l]:list_off[l+1]``
 * ``ids``      n int32 base ids, list-contiguous (``ivf[l].ids``)
 * ``codes``    n x m uint8 (``ivf[l].codes``; exact when ks <= 256)
+* ``pq2``, ``codes2`` (optional) refinement quantizer of the residual error
+  x - y_list - c1(codes): m2 x 256 x d/m2 float32 and n x m2 uint8 codes in
+  the row order of ``codes`` (no counterpart in the reference)
 """
 from __future__ import annotations
 
@@ -26,6 +29,8 @@ class IVFPQData:
     list_off: np.ndarray
     ids: np.ndarray
     codes: np.ndarray
+    pq2: np.ndarray | None = None
+    codes2: np.ndarray | None = None
 
     @property
     def d(self) -> int:
@@ -68,6 +73,14 @@ class IVFPQData:
             raise ValueError("ids / codes do not match list_off")
         if n and int(self.codes.max()) >= ks:
             raise ValueError("code value >= ks")
+        if (self.pq2 is None) != (self.codes2 is None):
+            raise ValueError("pq2 and codes2 go together")
+        if self.pq2 is not None:
+            m2 = self.pq2.shape[0]
+            if self.pq2.shape != (m2, 256, d // m2) or m2 * (d // m2) != d:
+                raise ValueError(f"pq2 shape {self.pq2.shape}")
+            if self.codes2.shape != (n, m2):
+                raise ValueError("codes2 does not match the codes")
 
     @staticmethod
     def from_reference_lists(coa, pq, list_sizes, ids, codes_i32) -> "IVFPQData":
@@ -91,12 +104,16 @@ class IVFPQData:
         return out
 
     def save(self, path: str) -> None:
-        np.savez_compressed(path, coa=self.coa, pq=self.pq, list_off=self.list_off, ids=self.ids, codes=self.codes)
+        extra = {} if self.pq2 is None else dict(pq2=self.pq2, codes2=self.codes2)
+        np.savez_compressed(path, coa=self.coa, pq=self.pq, list_off=self.list_off, ids=self.ids, codes=self.codes,
+                            **extra)
 
     @staticmethod
     def load(path: str) -> "IVFPQData":
         z = np.load(path)
         out = IVFPQData(coa=z["coa"], pq=z["pq"], list_off=z["list_off"].astype(np.int64),
-                        ids=z["ids"].astype(np.int32), codes=z["codes"].astype(np.uint8))
+                        ids=z["ids"].astype(np.int32), codes=z["codes"].astype(np.uint8),
+                        pq2=z["pq2"] if "pq2" in z else None,
+                        codes2=z["codes2"].astype(np.uint8) if "codes2" in z else None)
         out.validate()
         return out
