@@ -74,6 +74,14 @@ int gbivf_index_create(gbivf_index **out, int device, int d, int coarsek, const 
                        int nsq, int ks, const float *pq, const int64_t *list_off,
                        const int32_t *ids, const uint8_t *codes);
 
+/* gbivf_index_create with the lists already in device memory (d_ids: n int32,
+ * d_codes: n x nsq bytes, list order as list_off gives it; ks must be 256):
+ * for indexes built on the GPU, where a host copy of billions of codes would
+ * be the slowest step. coa, pq and list_off are host arrays. */
+int gbivf_index_create_device(gbivf_index **out, int device, int d, int coarsek, const float *coa, int nsq, int ks,
+                              const float *pq, const int64_t *list_off, const int32_t *d_ids,
+                              const uint8_t *d_codes);
+
 /* Upload an index given as the reference holds it: ivfpq_t fields plus one
  * ivf_t per list (ids, idstam, int32 codes n x nsq).
  * pq_centroids[s] is the ks x ds array of sub-quantizer s (pqtipo.centroids,
@@ -261,6 +269,13 @@ int gbivf_kmeans(const float *d_x, int64_t n, int d, int k, int niter, uint64_t 
 /* Nearest of k centroids for each of n rows (d = 128, or 8, 16, 32). */
 int gbivf_assign(const float *d_x, int64_t n, int d, const float *d_centroids, int k,
                  int32_t *d_assign, void *stream);
+
+/* gbivf_assign with flags: GBIVF_ASSIGN_BF16 (d = 128) compares against the
+ * centroids rounded to BF16 -- half the tensor-core work of the default
+ * split form, and not always the nearest centroid: for bulk index building. */
+#define GBIVF_ASSIGN_BF16 0x1u
+int gbivf_assign_flags(const float *d_x, int64_t n, int d, const float *d_centroids, int k, int32_t *d_assign,
+                       unsigned flags, void *stream);
 
 /* Sub-quantizers: m k-means of 256 centroids on the sub-vectors of the
  * residuals d_r (n x d); d_pq receives m x 256 x (d/m). */

@@ -30,7 +30,8 @@ EXPORTS = [
     "gbivf_search_batched", "gbivf_search_batched_device", "gbivf_graph_capture", "gbivf_graph_launch",
     "gbivf_graph_destroy", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
     "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats", "gbivf_coarse_assign_device",
-    "gbivf_index_set_refine", "gbivf_index_set_refine_device", "gbivf_pq_error",
+    "gbivf_index_set_refine", "gbivf_index_set_refine_device", "gbivf_pq_error", "gbivf_index_create_device",
+    "gbivf_assign_flags",
 ]
 
 
@@ -73,6 +74,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_index_set_refine.argtypes = [vp, i32, i32, vp, vp]
     lib.gbivf_index_set_refine_device.argtypes = [vp, i32, i32, vp, vp]
     lib.gbivf_pq_error.argtypes = [vp, i64, i32, vp, vp, i32, vp, vp, vp, vp]
+    lib.gbivf_index_create_device.argtypes = [C.POINTER(vp), i32, i32, i32, vp, i32, i32, vp, vp, vp, vp]
+    lib.gbivf_assign_flags.argtypes = [vp, i64, i32, vp, i32, vp, u32, vp]
     lib.gbivf_search_batched.argtypes = [vp, vp, i32, vp, vp, u32, vp, vp]
     lib.gbivf_search_batched_device.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, u32, vp, vp, vp]
     lib.gbivf_graph_capture.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]

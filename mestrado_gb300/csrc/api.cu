@@ -135,13 +135,14 @@ struct gbivf_index {
 
 namespace {
 
+// allocate `count` elements owned by the index and copy them from the host (h may be NULL: allocate only)
 template <class T>
 cudaError_t upload(gbivf_index* ix, const T* h, size_t count, T** out) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
     if (e != cudaSuccess) return e;
     ix->owned.push_back(p);
-    if (count) e = cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+    if (count && h) e = cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
     *out = static_cast<T*>(p);
     return e;
 }
@@ -162,7 +163,8 @@ void free_index(gbivf_index* ix) {
 }
 
 int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
-                const float* pq, const int64_t* list_off, const int32_t* ids, const uint8_t* codes) {
+                const float* pq, const int64_t* list_off, const int32_t* ids, const uint8_t* codes,
+                bool dev_lists = false) {
     if (!out) return fail(GBIVF_ERR_INVALID, "out is NULL");
     *out = nullptr;
     if (d <= 0 || nsq <= 0 || d % nsq) return fail(GBIVF_ERR_INVALID, "d=%d must be a positive multiple of nsq=%d", d, nsq);
@@ -175,8 +177,12 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         if (list_off[l + 1] < list_off[l]) return fail(GBIVF_ERR_INVALID, "list_off decreases at list %d", l);
     const int64_t n = list_off[coarsek];
     if (n > 0 && (!ids || !codes)) return fail(GBIVF_ERR_INVALID, "NULL ids/codes");
-    for (int64_t i = 0; i < n * nsq; i++)
-        if (codes[i] >= ks) return fail(GBIVF_ERR_INVALID, "code %d >= ks=%d at byte %lld", codes[i], ks, (long long)i);
+    if (dev_lists && ks != 256)
+        return fail(GBIVF_ERR_UNSUPPORTED, "device-resident lists need ks = 256 (every byte is a valid code)");
+    if (!dev_lists)
+        for (int64_t i = 0; i < n * nsq; i++)
+            if (codes[i] >= ks)
+                return fail(GBIVF_ERR_INVALID, "code %d >= ks=%d at byte %lld", codes[i], ks, (long long)i);
     for (int l = 0; l < coarsek; l++)
         if (list_off[l + 1] - list_off[l] > 0x7fffffffLL) return fail(GBIVF_ERR_UNSUPPORTED, "list %d too long", l);
     if (n > 0xffffffffLL) return fail(GBIVF_ERR_UNSUPPORTED, "more than 2^32 vectors");
@@ -189,9 +195,20 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
 
     auto* ix = new gbivf_index();
     ix->device = device;
-    for (int64_t i = 0; i < n; i++) {
-        if (i == 0 || ids[i] < ix->min_id) ix->min_id = ids[i];
-        if (i == 0 || ids[i] > ix->max_id) ix->max_id = ids[i];
+    if (!dev_lists) {
+        for (int64_t i = 0; i < n; i++) {
+            if (i == 0 || ids[i] < ix->min_id) ix->min_id = ids[i];
+            if (i == 0 || ids[i] > ix->max_id) ix->max_id = ids[i];
+        }
+    } else if (n > 0) {
+        int range[2];
+        cudaError_t e = launch_id_range(ids, n, range, 0);
+        if (e != cudaSuccess) {
+            delete ix;
+            return cuda_fail(e, "id range");
+        }
+        ix->min_id = range[0];
+        ix->max_id = range[1];
     }
     const int ds = d / nsq;
     // list starts aligned so that a list's first code row sits on 16 bytes
@@ -209,13 +226,17 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     }
     rows = (rows + align_rows - 1) / align_rows * align_rows;
     ix->h_beg = beg;
-    std::vector<uint8_t> pcodes((size_t)std::max<int64_t>(rows, 1) * nsq, 0);
-    std::vector<int32_t> pids((size_t)std::max<int64_t>(rows, 1), -1);
-    for (int l = 0; l < coarsek; l++) {
-        int64_t len = ix->h_len[l];
-        if (!len) continue;
-        memcpy(&pcodes[(size_t)beg[l] * nsq], codes + list_off[l] * nsq, (size_t)len * nsq);
-        memcpy(&pids[(size_t)beg[l]], ids + list_off[l], (size_t)len * sizeof(int32_t));
+    std::vector<uint8_t> pcodes;
+    std::vector<int32_t> pids;
+    if (!dev_lists) {
+        pcodes.assign((size_t)std::max<int64_t>(rows, 1) * nsq, 0);
+        pids.assign((size_t)std::max<int64_t>(rows, 1), -1);
+        for (int l = 0; l < coarsek; l++) {
+            int64_t len = ix->h_len[l];
+            if (!len) continue;
+            memcpy(&pcodes[(size_t)beg[l] * nsq], codes + list_off[l] * nsq, (size_t)len * nsq);
+            memcpy(&pids[(size_t)beg[l]], ids + list_off[l], (size_t)len * sizeof(int32_t));
+        }
     }
     std::vector<float> cn(coarsek);
     for (int c = 0; c < coarsek; c++) cn[c] = norm_f_host(coa + (int64_t)c * d, d);
@@ -250,9 +271,31 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         (e = upload(ix, plo.data(), plo.size(), &p_plo)) != cudaSuccess ||
         (e = upload(ix, beg.data(), beg.size(), &p_beg)) != cudaSuccess ||
         (e = upload(ix, ix->h_len.data(), ix->h_len.size(), &p_len)) != cudaSuccess ||
-        (e = upload(ix, pcodes.data(), pcodes.size(), &p_codes)) != cudaSuccess ||
-        (e = upload(ix, pids.data(), pids.size(), &p_ids)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        free_index(ix);
+        delete ix;
+        return cuda_fail(e, "index upload");
+    }
+    if (!dev_lists) {
+        e = upload(ix, pcodes.data(), pcodes.size(), &p_codes);
+        if (e == cudaSuccess) e = upload(ix, pids.data(), pids.size(), &p_ids);
+    } else {
+        // device-resident lists: padded buffers, then one scatter per array (no host copy)
+        const size_t nr = (size_t)std::max<int64_t>(rows, 1);
+        int64_t *d_off = nullptr, *d_beg = nullptr;
+        e = upload(ix, (const uint8_t*)nullptr, nr * nsq, &p_codes);
+        if (e == cudaSuccess) e = upload(ix, (const int32_t*)nullptr, nr, &p_ids);
+        if (e == cudaSuccess) e = upload(ix, list_off, (size_t)coarsek + 1, &d_off);
+        if (e == cudaSuccess) e = upload(ix, beg.data(), beg.size(), &d_beg);
+        if (e == cudaSuccess) e = cudaMemset(p_codes, 0, nr * nsq);
+        if (e == cudaSuccess) e = cudaMemset(p_ids, 0xff, nr * sizeof(int32_t));
+        if (e == cudaSuccess) e = launch_scatter_rows(codes, d_off, d_beg, coarsek, nsq, p_codes, 0);
+        if (e == cudaSuccess)
+            e = launch_scatter_rows(reinterpret_cast<const uint8_t*>(ids), d_off, d_beg, coarsek, 4,
+                                    reinterpret_cast<uint8_t*>(p_ids), 0);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
         free_index(ix);
         delete ix;
         return cuda_fail(e, "index upload");
@@ -613,6 +656,12 @@ int gbivf_version(void) { return 1; }
 int gbivf_index_create(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
                        const float* pq, const int64_t* list_off, const int32_t* ids, const uint8_t* codes) {
     return create_impl(out, device, d, coarsek, coa, nsq, ks, pq, list_off, ids, codes);
+}
+
+int gbivf_index_create_device(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq, int ks,
+                              const float* pq, const int64_t* list_off, const int32_t* d_ids, const uint8_t* d_codes) {
+    if (list_off && list_off[coarsek] > 0 && (!d_ids || !d_codes)) return fail(GBIVF_ERR_INVALID, "NULL device lists");
+    return create_impl(out, device, d, coarsek, coa, nsq, ks, pq, list_off, d_ids, d_codes, true);
 }
 
 int gbivf_index_create_from_lists(gbivf_index** out, int device, int d, int coarsek, const float* coa, int nsq,
@@ -1280,6 +1329,21 @@ int gbivf_kmeans(const float* d_x, int64_t n, int d, int k, int niter, uint64_t 
     if (d != 128 && d != 8 && d != 16 && d != 32)
         return fail(GBIVF_ERR_UNSUPPORTED, "k-means on the GPU takes d = 128 (tensor cores) or 8, 16, 32");
     CK(kmeans_rows(d_x, n, d, d, k, niter, seed, d_centroids, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_assign_flags(const float* d_x, int64_t n, int d, const float* d_centroids, int k, int32_t* d_assign,
+                       unsigned flags, void* stream) {
+    if (!d_x || !d_centroids || !d_assign || n < 0 || k <= 0) return fail(GBIVF_ERR_INVALID, "bad assign arguments");
+    if (flags & ~GBIVF_ASSIGN_BF16) return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if (d != 128 && d != 8 && d != 16 && d != 32)
+        return fail(GBIVF_ERR_UNSUPPORTED, "assignment on the GPU takes d = 128 or 8, 16, 32");
+    if (n == 0) return GBIVF_OK;
+    cudaError_t e = assign_rows(d_x, n, d, d, d_centroids, k, d_assign, (cudaStream_t)stream,
+                                (flags & GBIVF_ASSIGN_BF16) != 0);
+    if (e == cudaErrorLaunchTimeout) return fail(GBIVF_ERR_TIMEOUT, "tensor-core assignment: a bounded wait ran out");
+    CK(e);
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
     return GBIVF_OK;
 }
 

@@ -207,22 +207,27 @@ inline unsigned blocks(int64_t work, int nt) { return (unsigned)((work + nt - 1)
 
 // nearest centroid for every row: tensor cores for d = 128, SIMT for d <= 32
 cudaError_t assign_rows(const float* x, int64_t n, int64_t ld, int d, const float* cent, int k, int32_t* assign,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool hi_only) {
     cudaError_t e = cudaSuccess;
     if (d == 128 && ld == 128) {
-        const int tiles = coarse_mma_ctiles(k);
-        const int64_t bq = std::max<int64_t>(MMA_QUERY_TILE, std::min<int64_t>(n, (1 << 24) / std::max(tiles, 1)) /
-                                                                  MMA_QUERY_TILE * MMA_QUERY_TILE);
-        void *ctiles = nullptr, *cnorm = nullptr, *qtiles = nullptr, *qn = nullptr, *part = nullptr, *err = nullptr;
+        // the persistent tcgen05 GEMM with the argmin epilogue, blocks of up to 2^20 rows
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 1;
+        const int64_t bq = std::min<int64_t>(n, 1 << 20), tail = n % bq;
+        // partial-result slots for the largest need among the two block sizes used
+        size_t slots = (size_t)bq * 2 * coarse_gemm_nsplit((int)bq, k, sms, nullptr);
+        if (tail) slots = std::max(slots, (size_t)tail * 2 * coarse_gemm_nsplit((int)tail, k, sms, nullptr));
+        void *ctiles = nullptr, *cnorm = nullptr, *qtiles = nullptr, *part = nullptr, *err = nullptr;
         auto cleanup = [&]() {
-            for (void* p : {ctiles, cnorm, qtiles, qn, part, err})
+            for (void* p : {ctiles, cnorm, qtiles, part, err})
                 if (p) cudaFree(p);
         };
+        const size_t qtb = coarse_gemm_qtile_bytes((int)bq);
         if ((e = cudaMalloc(&ctiles, coarse_mma_tile_bytes(k, true))) != cudaSuccess ||
             (e = cudaMalloc(&cnorm, sizeof(float) * k)) != cudaSuccess ||
-            (e = cudaMalloc(&qtiles, coarse_mma_tile_bytes((int)bq, false))) != cudaSuccess ||
-            (e = cudaMalloc(&qn, sizeof(double) * bq)) != cudaSuccess ||
-            (e = cudaMalloc(&part, sizeof(u64) * bq * tiles)) != cudaSuccess ||
+            (e = cudaMalloc(&qtiles, qtb)) != cudaSuccess ||
+            (e = cudaMalloc(&part, sizeof(u64) * slots)) != cudaSuccess ||
             (e = cudaMalloc(&err, sizeof(int))) != cudaSuccess) {
             cleanup();
             return e;
@@ -232,13 +237,16 @@ cudaError_t assign_rows(const float* x, int64_t n, int64_t ld, int d, const floa
         if (e == cudaSuccess) e = launch_norm_f(cent, k, d, (float*)cnorm, st);
         for (int64_t r0 = 0; r0 < n && e == cudaSuccess; r0 += bq) {
             const int nb = (int)std::min<int64_t>(bq, n - r0);
-            e = launch_norm_d(x + r0 * d, nb, d, (double*)qn, st);
-            if (e == cudaSuccess) e = launch_bf16_tiles(x + r0 * d, nb, MMA_QUERY_TILE, (uint8_t*)qtiles, st);
+            const int ns = coarse_gemm_nsplit(nb, k, sms, nullptr);
+            e = launch_bf16_tiles(x + r0 * d, nb, MMA_QUERY_TILE, (uint8_t*)qtiles, st);
+            const size_t written = coarse_mma_tile_bytes(nb, false), total = coarse_gemm_qtile_bytes(nb);
+            if (e == cudaSuccess && total > written)
+                e = cudaMemsetAsync((uint8_t*)qtiles + written, 0, total - written, st);
             if (e == cudaSuccess)
-                e = launch_coarse_mma((uint8_t*)qtiles, (uint8_t*)ctiles, nb, k, (double*)qn, (float*)cnorm, nullptr,
-                                      (int*)err, st, (u64*)part);
+                e = launch_coarse_gemm_argmin((uint8_t*)qtiles, (uint8_t*)ctiles, nb, k, (float*)cnorm, (u64*)part,
+                                              sms, (int*)err, st, hi_only);
             if (e == cudaSuccess) {
-                argmin_reduce_kernel<<<blocks(nb, 256), 256, 0, st>>>((u64*)part, nb, tiles, assign + r0);
+                argmin_reduce_kernel<<<blocks(nb, 256), 256, 0, st>>>((u64*)part, nb, 2 * ns, assign + r0);
                 e = cudaGetLastError();
             }
         }

@@ -18,7 +18,8 @@
 //     the other accumulator pair meanwhile. Store mode writes approximate
 //     distances. Chunk-minimum mode writes, per query and 32 centroids, the
 //     smallest upper bound approx + eps (the sample of the filtered stage).
-//     Filter mode tests each (query, centroid) against the query's bound T
+//     Argmin mode keeps, per query, the nearest centroid of its range (index
+//     building). Filter mode tests each (query, centroid) against the query's bound T
 //     with a three-operation pre-test, acc >= G_c - ||q|| K_c + H_q, the
 //     candidate test a - eps <= T solved for the accumulator (G_c = ||c||^2
 //     (1 - 2^-20) / 2, K_c = MIXED_EPS_REL ||c|| / 2, H_q from ||q||^2 and T
@@ -55,6 +56,8 @@ struct PgArgs {
     const float* cnorm = nullptr;
     float* out = nullptr;  // store: nq x ld approximate distances; chunk-min: nq x ld (ld >= C / 32)
     int64_t ld = 0;
+    unsigned long long* amin = nullptr;  // argmin: per (query, centroid range, column half) the best key
+    bool hi_only = false;                // argmin: c_hi tiles only (bf16 centroids; index building)
     CoarseFilter f;                // filter mode
     const float* colG = nullptr;   // nct * 128: ||c||^2 (1 - 2^-20) / 2, +inf past C
     const float* colK = nullptr;   // nct * 128: MIXED_EPS_REL ||c|| / 2, 0 past C
@@ -62,7 +65,7 @@ struct PgArgs {
     int* err = nullptr;
 };
 
-enum PgMode { PG_STORE = 0, PG_CHUNKMIN = 1, PG_FILTER = 2 };
+enum PgMode { PG_STORE = 0, PG_CHUNKMIN = 1, PG_FILTER = 2, PG_ARGMIN = 3 };
 
 // work item -> (query pair, first tile, end tile); items sharing a centroid range are adjacent
 __device__ __forceinline__ void pg_item(const PgArgs& p, int it, int& qp, int& t0, int& t1) {
@@ -77,7 +80,8 @@ __device__ __forceinline__ void pg_item(const PgArgs& p, int it, int& qp, int& t
 // gk_stride floats apart; filter: t_c = G_c - qlen_w K_c)
 template <int MODE>
 __device__ __forceinline__ void pg_chunk(const PgArgs& p, const uint32_t (&r)[32], const float* gs, int gk_stride,
-                                         int c0, int row, float qn, float qlen, float h, int2* sv, int& nsv) {
+                                         int c0, int row, float qn, float qlen, float h, int2* sv, int& nsv,
+                                         float& bv, int& bi) {
     if (MODE == PG_FILTER) {
         // gs holds t_c = G_c - qlen_w K_c with qlen_w >= this row's ||q|| (the warp's largest), so
         // acc - t_c >= h is implied by the row's exact candidate test; survivors (rare) go to this
@@ -93,6 +97,21 @@ __device__ __forceinline__ void pg_chunk(const PgArgs& p, const uint32_t (&r)[32
                     sv[min(nsv, p.f.sreg - 1)] = make_int2(c0 + 4 * q4 + e, (int)r[4 * q4 + e]);
                     nsv++;
                 }
+            }
+        }
+    } else if (MODE == PG_ARGMIN) {
+        // nearest centroid: ||c||^2 - 2 acc decides it (||q||^2 is the row's constant); ties keep
+        // the lower index (columns come in ascending order)
+#pragma unroll
+        for (int q4 = 0; q4 < 8; q4++) {
+            const float4 cn = reinterpret_cast<const float4*>(gs)[q4];
+            const float cv[4] = {cn.x, cn.y, cn.z, cn.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const float v = __fmaf_rn(-2.0f, __uint_as_float(r[4 * q4 + e]), cv[e]);
+                const bool better = v < bv && c0 + 4 * q4 + e < p.C;
+                bv = better ? v : bv;
+                bi = better ? c0 + 4 * q4 + e : bi;
             }
         }
     } else if (MODE == PG_CHUNKMIN) {
@@ -197,8 +216,9 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&b_full[s], B_TILE_BYTES);
-                    bulk_load(sB + s * B_TILE_BYTES, p.ctiles + (int64_t)t * B_TILE_BYTES, B_TILE_BYTES, &b_full[s]);
+                    const uint32_t bbytes = p.hi_only ? B_HALF_BYTES : B_TILE_BYTES;
+                    mbar_expect_tx(&b_full[s], bbytes);
+                    bulk_load(sB + s * B_TILE_BYTES, p.ctiles + (int64_t)t * B_TILE_BYTES, bbytes, &b_full[s]);
                     armed_b[s] = u;
                 }
             }
@@ -238,8 +258,10 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                     for (int j = 0; j < PG_QT; j++) {
                         const uint32_t d = tmem + (uint32_t)((s * PG_QT + j) * MM_N);
                         const uint32_t a0 = smem_addr(sA + j * A_TILE_BYTES);
+                        const int steps = p.hi_only ? MM_K / 16 : 2 * (MM_K / 16);
 #pragma unroll
                         for (int step = 0; step < 2 * (MM_K / 16); step++) {
+                            if (step >= steps) break;
                             const int k = step % (MM_K / 16), half = step / (MM_K / 16);
                             mma_bf16(d, make_smem_desc(a0 + k * 2 * CORE_LBO),
                                      make_smem_desc(b0 + half * B_HALF_BYTES + k * 2 * CORE_LBO), MMA_IDESC,
@@ -278,7 +300,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
             for (int j = 0; j < PG_QT; j++) {
                 row[j] = qp * (PG_QT * MM_M) + j * MM_M + qd * 32 + lane;
                 const bool valid = row[j] < p.nq;
-                qn[j] = valid ? (float)p.qnorm[row[j]] : 0.0f;
+                qn[j] = (valid && MODE != PG_ARGMIN) ? (float)p.qnorm[row[j]] : 0.0f;
                 qlen[j] = sqrtf(qn[j]);
                 T[j] = 0.0f;
                 h[j] = __int_as_float(0x7f800000);
@@ -296,8 +318,12 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
             const int sp = it / p.nqp;
             int2* sv[PG_QT];
             int nsv[PG_QT];
+            float bv[PG_QT];  // argmin: best ||c||^2 - 2 acc and its centroid
+            int bi[PG_QT];
 #pragma unroll
             for (int j = 0; j < PG_QT; j++) {
+                bv[j] = __int_as_float(0x7f800000);
+                bi[j] = 0;
                 nsv[j] = 0;
                 sv[j] = (MODE == PG_FILTER && row[j] < p.nq)
                             ? p.f.surv + (((int64_t)row[j] * p.nsplit + sp) * 2 + hf) * p.f.sreg
@@ -312,7 +338,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                 // this warp's 64 column terms, fetched before the wait
                 const int cb = t * MM_N + hf * 64;
                 float2 gv, kv = make_float2(0.0f, 0.0f);
-                if (MODE != PG_STORE) {
+                if (MODE == PG_CHUNKMIN || MODE == PG_FILTER) {
                     gv = __ldg(reinterpret_cast<const float2*>(p.colG + cb) + lane);
                     kv = __ldg(reinterpret_cast<const float2*>(p.colK + cb) + lane);
                 } else if (cb + 2 * lane + 1 < p.C) {
@@ -333,7 +359,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                         make_float2(__fmaf_rn(-qlen_w, kv.x, gv.x), __fmaf_rn(-qlen_w, kv.y, gv.y));
                 } else {
                     reinterpret_cast<float2*>(gs)[lane] = gv;
-                    if (MODE != PG_STORE) reinterpret_cast<float2*>(gs + 64)[lane] = kv;
+                    if (MODE == PG_CHUNKMIN) reinterpret_cast<float2*>(gs + 64)[lane] = kv;
                 }
                 __syncwarp();
 #pragma unroll
@@ -343,8 +369,9 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                     tmem_ld32_async(ta, ra);
                     tmem_ld32_async(ta + 32, rb);
                     tmem_wait_ld();
-                    pg_chunk<MODE>(p, ra, gs, 64, cb, row[j], qn[j], qlen[j], h[j], sv[j], nsv[j]);
-                    pg_chunk<MODE>(p, rb, gs + 32, 64, cb + 32, row[j], qn[j], qlen[j], h[j], sv[j], nsv[j]);
+                    pg_chunk<MODE>(p, ra, gs, 64, cb, row[j], qn[j], qlen[j], h[j], sv[j], nsv[j], bv[j], bi[j]);
+                    pg_chunk<MODE>(p, rb, gs + 32, 64, cb + 32, row[j], qn[j], qlen[j], h[j], sv[j], nsv[j], bv[j],
+                                   bi[j]);
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -354,6 +381,11 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
 #pragma unroll
                 for (int j = 0; j < PG_QT; j++)
                     if (row[j] < p.nq) p.f.scnt[((int64_t)row[j] * p.nsplit + sp) * 2 + hf] = nsv[j];
+            }
+            if (MODE == PG_ARGMIN && ok) {
+#pragma unroll
+                for (int j = 0; j < PG_QT; j++)
+                    if (row[j] < p.nq) p.amin[((int64_t)row[j] * p.nsplit + sp) * 2 + hf] = make_key(bv[j], (uint32_t)bi[j]);
             }
         }
         if (!ok && lane == 0) {
@@ -407,6 +439,7 @@ static cudaError_t launch_pg(PgArgs& p, int mode, int num_sms, cudaStream_t st) 
     switch (mode) {
         case PG_STORE: return launch_pg_mode<PG_STORE>(p, grid, st);
         case PG_CHUNKMIN: return launch_pg_mode<PG_CHUNKMIN>(p, grid, st);
+        case PG_ARGMIN: return launch_pg_mode<PG_ARGMIN>(p, grid, st);
         default: return launch_pg_mode<PG_FILTER>(p, grid, st);
     }
 }
@@ -446,6 +479,21 @@ cudaError_t launch_coarse_gemm_chunkmin(const uint8_t* qtiles, const uint8_t* ct
     p.ld = ld;
     p.err = err;
     return launch_pg(p, PG_CHUNKMIN, num_sms, st);
+}
+
+cudaError_t launch_coarse_gemm_argmin(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C, const float* cnorm,
+                                      unsigned long long* part, int num_sms, int* err, cudaStream_t st, bool hi_only) {
+    if (!part) return cudaErrorInvalidValue;
+    PgArgs p;
+    p.hi_only = hi_only;
+    p.qtiles = qtiles;
+    p.ctiles = ctiles;
+    p.nq = nq;
+    p.C = C;
+    p.cnorm = cnorm;
+    p.amin = part;
+    p.err = err;
+    return launch_pg(p, PG_ARGMIN, num_sms, st);
 }
 
 cudaError_t launch_coarse_gemm_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,

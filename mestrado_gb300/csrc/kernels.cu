@@ -136,6 +136,38 @@ cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const 
     return cudaGetLastError();
 }
 
+__global__ void id_range_kernel(const int32_t* __restrict__ ids, int64_t n, int* __restrict__ range) {
+    int lo = 0x7fffffff, hi = (int)0x80000000;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        lo = min(lo, ids[i]);
+        hi = max(hi, ids[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&range[0], lo);
+        atomicMax(&range[1], hi);
+    }
+}
+
+cudaError_t launch_id_range(const int32_t* ids, int64_t n, int* range, cudaStream_t st) {
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 2 * sizeof(int));
+    if (e != cudaSuccess) return e;
+    const int init[2] = {0x7fffffff, (int)0x80000000};
+    e = cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        id_range_kernel<<<1024, 256, 0, st>>>(ids, n, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(range, d, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    return e;
+}
+
 // one CTA per list: copy its rows from the caller's order into the padded row layout
 __global__ void scatter_rows_kernel(const uint8_t* __restrict__ src, const int64_t* __restrict__ off,
                                     const int64_t* __restrict__ beg, int width, uint8_t* __restrict__ dst) {

@@ -101,6 +101,8 @@ bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
 
+// [min, max] of n int32 values on the device, returned to the host (synchronises the stream)
+cudaError_t launch_id_range(const int32_t* ids, int64_t n, int* range, cudaStream_t st);
 // rows of `width` bytes in list order (list l: rows off[l] .. off[l+1]) -> dst rows beg[l] ..
 cudaError_t launch_scatter_rows(const uint8_t* src, const int64_t* off, const int64_t* beg, int C, int width,
                                 uint8_t* dst, cudaStream_t st);
@@ -177,6 +179,12 @@ cudaError_t launch_coarse_gemm_chunkmin(const uint8_t* qtiles, const uint8_t* ct
                                         cudaStream_t st);
 // centroid ranges per 256-query tile pair the persistent GEMM uses for (nq, C)
 int coarse_gemm_nsplit(int nq, int C, int num_sms, int* split_tiles);
+// nearest centroid by the approximate distance: part[q * 2 * nsplit + g] = the best key of each
+// (centroid range, column half) g, nsplit = coarse_gemm_nsplit(nq, C, num_sms)
+// (hi_only: the c_hi tiles alone, half the work, for index building)
+cudaError_t launch_coarse_gemm_argmin(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C, const float* cnorm,
+                                      unsigned long long* part, int num_sms, int* err, cudaStream_t st,
+                                      bool hi_only = false);
 // the mixed form's filtered pass (f.surv / f.scnt / f.sreg / f.nsplit as above);
 // cn_max / clen_max: maxima of cnorm / f.clen
 cudaError_t launch_coarse_gemm_filter(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
@@ -199,8 +207,9 @@ cudaError_t launch_coarse_cand_select(const DevIndex& ix, const float* q, const 
                                       cudaStream_t st);
 
 // index building (build_gpu.cu); synchronous, allocate their own temporaries
+// (hi_only, d = 128: centroids rounded to BF16 -- faster, not always the nearest; bulk index building)
 cudaError_t assign_rows(const float* x, int64_t n, int64_t ld, int d, const float* cent, int k, int32_t* assign,
-                        cudaStream_t st);
+                        cudaStream_t st, bool hi_only = false);
 cudaError_t kmeans_rows(const float* x, int64_t n, int64_t ld, int d, int k, int niter, uint64_t seed, float* cent,
                         cudaStream_t st);
 cudaError_t gen_mixture(float* out, int64_t n, int d, const float* means, int ncomp, const double* cdf, float sigma,

@@ -53,6 +53,28 @@ class GpuIndex:
             self.set_base(base)
 
     @classmethod
+    def from_device(cls, coa, pq, list_off, d_ids, d_codes, pq2=None, d_codes2=None, device: int = 0) -> "GpuIndex":
+        """An index whose lists are already in device memory (torch tensors in list
+        order: d_ids n int32, d_codes n x m uint8, optional refinement codebook pq2
+        (host) and codes d_codes2 n x m2): no host copy of the codes."""
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.data = None
+        self.device = device
+        self.base_rows = 0
+        h = C.c_void_p()
+        keep = [_c(coa, np.float32), _c(pq, np.float32), _c(list_off, np.int64)]
+        check(self.lib.gbivf_index_create_device(C.byref(h), device, coa.shape[1], coa.shape[0], _p(keep[0]),
+                                                 pq.shape[0], pq.shape[1], _p(keep[1]), _p(keep[2]),
+                                                 C.c_void_p(d_ids.data_ptr()), C.c_void_p(d_codes.data_ptr())))
+        self.h = h
+        if pq2 is not None:
+            p2 = _c(pq2, np.float32)
+            check(self.lib.gbivf_index_set_refine_device(h, pq2.shape[0], 256, _p(p2),
+                                                         C.c_void_p(d_codes2.data_ptr())))
+        return self
+
+    @classmethod
     def from_handle(cls, h: C.c_void_p, device: int = 0) -> "GpuIndex":
         self = cls.__new__(cls)
         self.lib = _lib.load()

@@ -171,6 +171,95 @@ def build_index_gpu(base, train, coarsek: int, m: int, niter: int = 10, seed: in
     return out
 
 
+def build_index_streaming(gm: GpuMixture, nbase: int, train, coarsek: int, m: int, m2: int = 0, niter: int = 10,
+                          seed: int = 0, chunk: int = 1 << 24, bf16_assign: bool = True, log=None):
+    """An index over a generated base too large to hold in memory (1B x 128
+    floats is 512 GB): chunks of the base are generated, assigned, PQ-encoded
+    and refinement-encoded on the fly; the lists are bucketed on the GPU (a
+    stable sort by list) and the index is created from those device arrays.
+    Returns (GpuIndex, list_off)."""
+    import time
+
+    import torch
+
+    from .engine import GpuIndex
+
+    lib = _lib.load()
+    dev = train.device
+    d = train.shape[1]
+    t0 = time.time()
+    coa, pq = train_quantizers(train, coarsek, m, niter, seed)
+    pq2 = train_refine(train, coa, pq, m2, niter, seed) if m2 else None
+    torch.cuda.synchronize()
+    if log:
+        log(f"quantizers trained in {time.time() - t0:.1f}s")
+    assign = torch.empty(nbase, dtype=torch.int32, device=dev)
+    codes = torch.empty((nbase, m), dtype=torch.uint8, device=dev)
+    codes2 = torch.empty((nbase, m2), dtype=torch.uint8, device=dev) if m2 else None
+    buf = torch.empty((min(chunk, nbase), d), dtype=torch.float32, device=dev)
+    err = torch.empty_like(buf) if m2 else None
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    t1 = time.time()
+    for r in range(0, nbase, chunk):
+        nb = min(chunk, nbase - r)
+        x = gm.generate(nb, stream_id=1, row0=r, out=buf[:nb])
+        a = assign[r:r + nb]
+        check(lib.gbivf_assign_flags(_ptr(x), nb, d, _ptr(coa), coarsek, _ptr(a), 1 if bf16_assign else 0, s))
+        check(lib.gbivf_pq_encode(_ptr(x), nb, d, _ptr(a), _ptr(coa), m, _ptr(pq), _ptr(codes[r:r + nb]), s))
+        if m2:
+            e = err[:nb]
+            check(lib.gbivf_pq_error(_ptr(x), nb, d, _ptr(a), _ptr(coa), m, _ptr(pq), _ptr(codes[r:r + nb]),
+                                     _ptr(e), s))
+            check(lib.gbivf_pq_encode(_ptr(e), nb, d, C.c_void_p(0), C.c_void_p(0), m2, _ptr(pq2),
+                                      _ptr(codes2[r:r + nb]), s))
+    del buf, err
+    torch.cuda.synchronize()
+    if log:
+        log(f"{nbase:,} vectors generated, assigned and encoded in {time.time() - t1:.1f}s")
+    order = torch.sort(assign, stable=True).indices
+    counts = torch.bincount(assign, minlength=coarsek).cpu().numpy()
+    off = np.zeros(coarsek + 1, np.int64)
+    np.cumsum(counts, out=off[1:])
+    del assign
+    ids = order.to(torch.int32)
+    codes_s = codes[order]
+    del codes
+    codes2_s = codes2[order] if m2 else None
+    del codes2, order
+    torch.cuda.empty_cache()
+    gi = GpuIndex.from_device(coa.cpu().numpy(), pq.cpu().numpy(), off, ids, codes_s,
+                              None if pq2 is None else pq2.cpu().numpy(), codes2_s, device=dev.index or 0)
+    del ids, codes_s, codes2_s
+    torch.cuda.empty_cache()
+    if log:
+        log(f"index created in {time.time() - t0:.1f}s in all")
+    return gi, off
+
+
+def exact_topk_streaming(gm: GpuMixture, nbase: int, queries, k: int, chunk: int = 1 << 24):
+    """Brute-force top-k over a generated base, chunk by chunk (evaluation only;
+    exact in FP32 for byte-valued vectors, as exact_topk)."""
+    import torch
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    nq, d = queries.shape
+    dev = queries.device
+    qn = (queries * queries).sum(1, keepdim=True)
+    best_d = torch.full((nq, k), float("inf"), device=dev)
+    best_i = torch.full((nq, k), -1, dtype=torch.int64, device=dev)
+    buf = torch.empty((min(chunk, nbase), d), dtype=torch.float32, device=dev)
+    for r in range(0, nbase, chunk):
+        nb = min(chunk, nbase - r)
+        x = gm.generate(nb, stream_id=1, row0=r, out=buf[:nb])
+        dist = qn + (x * x).sum(1)[None, :] - 2.0 * (queries @ x.T)
+        vd, vi = torch.topk(dist, min(k, nb), dim=1, largest=False)
+        cd = torch.cat([best_d, vd], 1)
+        ci = torch.cat([best_i, vi + r], 1)
+        sel = torch.topk(cd, k, dim=1, largest=False).indices
+        best_d, best_i = torch.gather(cd, 1, sel), torch.gather(ci, 1, sel)
+    return best_i.cpu().numpy()
+
+
 def exact_topk(base, queries, k: int, batch: int = 256):
     """Brute-force top-k by squared L2 on the GPU. For byte-valued vectors (d <=
     256) every product and partial sum is an integer below 2^24, so FP32 gives
