@@ -50,6 +50,11 @@ CONFIGS = {
 # Larger workloads, generated and indexed on the GPU (gbivf_generate_mixture,
 # gbivf_kmeans, gbivf_pq_encode): the precision form against the plain one.
 LARGE = {
+    # billion scale with re-rank by refinement codes; the base is generated, assigned and encoded in
+    # chunks and never held (1B x 128 floats is 512 GB)
+    "cfg5": dict(d=128, ncomp=16384, seed=0, zipf=None, nbase=1_000_000_000, ntrain=2_621_440, nq=10_000,
+                 C=262144, m=8, m2=8, w=64, k=100, kl=1000, uneven=False, train_iters=6, recall_q=100,
+                 stream=True),
     # the 100M workload's shape at 1/5 scale (20M base, 65,536 Zipf lists, m = 16, uneven nprobe / k):
     # small enough to profile with every ncu section
     "cfg4s": dict(d=128, ncomp=65536, seed=0, zipf=1.1, nbase=20_000_000, ntrain=655_360, nq=8192,
@@ -504,6 +509,93 @@ def run_large(args, c, name, local_rank):
     gi.close()
 
 
+def run_stream(args, c, name, local_rank):
+    """Billion-scale configuration: streaming GPU build with refinement codes, both forms (plain
+    FP32; tensor-core coarse + precision-form scan) timed as CUDA-graph replays of one batch with
+    the refinement re-rank of the kl best ADC candidates; recall@1/10/100 against a brute-force
+    ground truth computed over the regenerated base."""
+    import torch
+
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_streaming, exact_topk_streaming
+    from mestrado_gb300.synth import Mixture
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    gm = GpuMixture(Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"], zipf=c["zipf"]))
+    t0 = time.time()
+    train = gm.generate(c["ntrain"], stream_id=2)
+    gi, off = build_index_streaming(gm, c["nbase"], train, c["C"], c["m"], m2=c["m2"], niter=c["train_iters"],
+                                    seed=c["seed"], log=log)
+    del train
+    torch.cuda.empty_cache()
+    t_build = time.time() - t0
+    nq, k, kl, w = c["nq"], c["k"], c["kl"], c["w"]
+    queries = gm.generate(nq, stream_id=3)
+    sample = 0 if args.no_recall else min(nq, c["recall_q"])
+    t0 = time.time()
+    gt = exact_topk_streaming(gm, c["nbase"], queries[:sample], k) if sample else None
+    t_gt = time.time() - t0
+    d_ids = torch.empty((nq, k), dtype=torch.int32, device=dev)
+    d_dis = torch.empty((nq, k), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    forms = {}
+    for form, mixed in (("plain", False), ("mixed", True)):
+        graph = gi.capture_graph(queries.data_ptr(), nq, k, w, d_ids.data_ptr(), d_dis.data_ptr(), kl=kl,
+                                 refine=True, mixed_coarse=mixed, mixed_scan=mixed, stream_ptr=sp)
+        for i in range(args.warmup):
+            graph.launch(sp)
+        stream.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks = ClockSampler(local_rank)
+        clocks.start()
+        total = 0.0
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xff)
+                ev0.record(stream)
+            graph.launch(sp)
+            with torch.cuda.stream(stream):
+                ev1.record(stream)
+            ev1.synchronize()
+            total += ev0.elapsed_time(ev1)
+        clk = clocks.stop()
+        graph.close()
+        ids = d_ids.cpu().numpy()
+        gi.search_device(queries.data_ptr(), nq, k, w, d_ids.data_ptr(), d_dis.data_ptr(), kl=kl, refine=True,
+                         stream_ptr=sp, profile=True, mixed_coarse=mixed, mixed_scan=mixed)
+        cm, sm = gi.last_stage_ms()
+        rec = {}
+        if sample:
+            for r in (1, 10, 100):
+                rec[f"recall@{r}"] = float(np.mean([len(set(ids[i, :r].tolist()) & set(gt[i, :r].tolist())) / r
+                                                    for i in range(sample)]))
+        forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps, coarse_ms=cm,
+                           scan_ms=sm, recall=rec, clocks=clk, ids=ids)
+    same_rows = float(np.mean([np.array_equal(a, b) for a, b in zip(forms["plain"]["ids"], forms["mixed"]["ids"])]))
+    mx = forms["mixed"]
+    wl = (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture, generated and encoded on the GPU "
+          f"in chunks), C={c['C']:,} lists, m={c['m']}x256 + m2={c['m2']}x256 refinement codes, {nq:,} queries/step, "
+          f"w={w}, k={k}, re-rank of the {kl} best ADC candidates by refinement codes")
+    line = {
+        "metric": "QPS", "value": mx["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 tensor-core coarse + fp32 re-check; fp16 tables, fp32 re-score",
+        "data": "synthetic",
+        "config": {"workload": wl, "form": "mixed, CUDA-graph replay", "plain_qps": forms["plain"]["qps"],
+                   "speedup_vs_plain": mx["qps"] / forms["plain"]["qps"], "identical_rows_fraction": same_rows,
+                   "recall_sample_queries": sample, "recall_mixed": mx["recall"],
+                   "recall_plain": forms["plain"]["recall"],
+                   "stage_ms_mixed": {"coarse": mx["coarse_ms"], "scan": mx["scan_ms"]},
+                   "stage_ms_plain": {"coarse": forms["plain"]["coarse_ms"], "scan": forms["plain"]["scan_ms"]},
+                   "index_build_s": t_build, "ground_truth_s": t_gt, "l2": "flushed between steps (256 MB write)"},
+        "clocks": mx["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    gi.close()
+
+
 def run_coarse(args, c, name, local_rank):
     """The coarse stage alone at a large configuration's shape (knn_full over C
     centroids, w nearest per query): plain FP32 and tensor-core forms, timed
@@ -595,6 +687,8 @@ def main():
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--stage", default="search", choices=["search", "coarse"],
                     help="large configurations: time the whole search, or the coarse stage alone")
+    ap.add_argument("--nbase", type=int, default=None,
+                    help="large configurations: override the base size (trial runs of a smaller base)")
     args = ap.parse_args()
     if args.warmup < 3:
         log(f"--warmup {args.warmup} raised to 3 (at least 3 untimed warm-up steps)")
@@ -602,6 +696,8 @@ def main():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.config in LARGE and args.nbase:
+        LARGE[args.config] = dict(LARGE[args.config], nbase=args.nbase)
     if args.config in LARGE:
         if args.impl == "reference" or world > 1:
             if rank == 0:
@@ -610,6 +706,8 @@ def main():
             return
         if args.stage == "coarse":
             run_coarse(args, LARGE[args.config], args.config, local_rank)
+        elif LARGE[args.config].get("stream"):
+            run_stream(args, LARGE[args.config], args.config, local_rank)
         else:
             run_large(args, LARGE[args.config], args.config, local_rank)
         return
