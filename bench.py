@@ -132,6 +132,13 @@ def ground_truth(base, queries, k, key, device):
     return out
 
 
+def stage_split(gi):
+    """Stage times of the index's last profiled search: coarse, scan (scan kernel + finalize) and the
+    two parts of the scan."""
+    cm, sk, fm = gi.last_stages_ms()
+    return {"coarse": cm, "scan": sk + fm, "scan_kernel": sk, "finalize": fm}
+
+
 def recall_report(ids, gt, k):
     hits = np.array([len(set(a[a >= 0].tolist()) & set(b[:k].tolist())) for a, b in zip(ids, gt)])
     # R@r as the reference prints it: share of queries whose true 1-NN is in the top r
@@ -303,7 +310,7 @@ def run_gpu(args, c, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     barrier()
-    step_ms, scan_ms, coarse_ms = [], [], []
+    step_ms, scan_ms, coarse_ms, scank_ms, fin_ms = [], [], [], [], []
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     for i in range(args.steps):
@@ -315,9 +322,11 @@ def run_gpu(args, c, rank, world, local_rank):
             ev1.record(stream)
         ev1.synchronize()
         step_ms.append(ev0.elapsed_time(ev1))
-        cm, sm = gi.last_stage_ms()
+        cm, sk, fm = gi.last_stages_ms()
         coarse_ms.append(cm)
-        scan_ms.append(sm)
+        scan_ms.append(sk + fm)
+        scank_ms.append(sk)
+        fin_ms.append(fm)
     barrier()
     clk = clocks.stop()
     total_ms = sum(step_ms)
@@ -353,7 +362,8 @@ def run_gpu(args, c, rank, world, local_rank):
         quality = recall_report(h_ids, gt, k)
 
     peak, peak_kind = measured_peak_hbm()
-    mean_scan_s = statistics.mean(scan_ms) / 1000.0
+    # the scan kernel alone (CUDA events on the engine's stream around its launch)
+    mean_scan_s = statistics.mean(scank_ms) / 1000.0
     achieved = scan_bytes / mean_scan_s / 1e9
     traffic = profiled_traffic(args.config)
     if rank == 0:
@@ -363,14 +373,16 @@ def run_gpu(args, c, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(c), "queries_per_step": nq, "parallelism": f"replica x{world}",
                        "l2": "flushed between steps (256 MB write)", **quality,
-                       "stage_ms": {"coarse": statistics.mean(coarse_ms), "scan": statistics.mean(scan_ms)}},
+                       "stage_ms": {"coarse": statistics.mean(coarse_ms), "scan": statistics.mean(scan_ms),
+                                    "scan_kernel": statistics.mean(scank_ms), "finalize": statistics.mean(fin_ms)}},
             "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(queries.nbytes),
                     "d2h_bytes_per_step": int(nq * k * 8)},
-            "roofline": {"bound": "hbm", "kernel": "ivf_scan_kernel", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "bytes_per_launch": scan_bytes, "traffic": traffic},
             "cpu_baseline": cpu,
-            "gpu_launches": 4 * args.steps,
+            # norm_d, coarse_dist, coarse_select, ivf_scan_persistent, finalize per search
+            "gpu_launches": 5 * args.steps,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -459,11 +471,11 @@ def run_large(args, c, name, local_rank):
         gi.lib.gbivf_search_batched_device(gi.h, C_ptr(queries), nq, C_ptr(d_w), C_ptr(d_k), C_ptr(d_off),
                                            max_w, max_k, 0x100 | (0x14 if mixed else 0), C_ptr(d_ids),
                                            C_ptr(d_dis), sp_ptr(sp))
-        cm, sm = gi.last_stage_ms()
+        stages = stage_split(gi)
         rec = [len(set(ids[off[i]:off[i] + kq[i]].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i]
                for i in range(sample)] or [float("nan")]
         forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps,
-                           coarse_ms=cm, scan_ms=sm, recall=float(np.mean(rec)), clocks=clk, ids=ids,
+                           stages=stages, recall=float(np.mean(rec)), clocks=clk, ids=ids,
                            dis=d_dis.cpu().numpy())
     pi, mi = forms["plain"]["ids"], forms["mixed"]["ids"]
     same_rows = float(np.mean([np.array_equal(pi[off[i]:off[i + 1]], mi[off[i]:off[i + 1]]) for i in range(nq)]))
@@ -479,7 +491,7 @@ def run_large(args, c, name, local_rank):
     same = same_rows == 1.0
     peak, peak_kind = measured_peak_hbm()
     mx = forms["mixed"]
-    achieved = scan_bytes / (mx["scan_ms"] / 1000.0) / 1e9
+    achieved = scan_bytes / (mx["stages"]["scan_kernel"] / 1000.0) / 1e9
     wl = (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture"
           f"{', Zipf ' + str(c['zipf']) if c['zipf'] else ''}), C={c['C']:,} lists, m={c['m']}x256, "
           f"{nq:,} queries/step, " + (f"nprobe log-uniform 1..{c['w']}, k in {{1,10,100,1000}}" if c["uneven"]
@@ -496,8 +508,7 @@ def run_large(args, c, name, local_rank):
                    "id_overlap_with_plain": overlap, "distance_mismatches_on_shared_ids": mismatch,
                    f"recall_sample_queries": sample,
                    "recall_mixed": mx["recall"], "recall_plain": forms["plain"]["recall"],
-                   "stage_ms_mixed": {"coarse": mx["coarse_ms"], "scan": mx["scan_ms"]},
-                   "stage_ms_plain": {"coarse": forms["plain"]["coarse_ms"], "scan": forms["plain"]["scan_ms"]},
+                   "stage_ms_mixed": mx["stages"], "stage_ms_plain": forms["plain"]["stages"],
                    "index_build_s": t_build, "generate_s": t_gen, "l2": "flushed between steps (256 MB write)"},
         "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": scan_bytes,
@@ -565,14 +576,14 @@ def run_stream(args, c, name, local_rank):
         ids = d_ids.cpu().numpy()
         gi.search_device(queries.data_ptr(), nq, k, w, d_ids.data_ptr(), d_dis.data_ptr(), kl=kl, refine=True,
                          stream_ptr=sp, profile=True, mixed_coarse=mixed, mixed_scan=mixed)
-        cm, sm = gi.last_stage_ms()
+        stages = stage_split(gi)
         rec = {}
         if sample:
             for r in (1, 10, 100):
                 rec[f"recall@{r}"] = float(np.mean([len(set(ids[i, :r].tolist()) & set(gt[i, :r].tolist())) / r
                                                     for i in range(sample)]))
-        forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps, coarse_ms=cm,
-                           scan_ms=sm, recall=rec, clocks=clk, ids=ids)
+        forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps, stages=stages,
+                           recall=rec, clocks=clk, ids=ids)
     same_rows = float(np.mean([np.array_equal(a, b) for a, b in zip(forms["plain"]["ids"], forms["mixed"]["ids"])]))
     mx = forms["mixed"]
     wl = (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture, generated and encoded on the GPU "
@@ -587,8 +598,7 @@ def run_stream(args, c, name, local_rank):
                    "speedup_vs_plain": mx["qps"] / forms["plain"]["qps"], "identical_rows_fraction": same_rows,
                    "recall_sample_queries": sample, "recall_mixed": mx["recall"],
                    "recall_plain": forms["plain"]["recall"],
-                   "stage_ms_mixed": {"coarse": mx["coarse_ms"], "scan": mx["scan_ms"]},
-                   "stage_ms_plain": {"coarse": forms["plain"]["coarse_ms"], "scan": forms["plain"]["scan_ms"]},
+                   "stage_ms_mixed": mx["stages"], "stage_ms_plain": forms["plain"]["stages"],
                    "index_build_s": t_build, "ground_truth_s": t_gt, "l2": "flushed between steps (256 MB write)"},
         "clocks": mx["clocks"],
     }

@@ -54,7 +54,9 @@ extern "C" {
 #define GBIVF_MIXED_SCAN_ALPHA 4
 #define GBIVF_RERANK_REFINE 0x20u /* re-rank the kl ADC candidates by the distance to their refined
                                      reconstruction y + c1(codes) + c2(refinement codes) instead of the
-                                     raw vectors (needs gbivf_index_set_refine; k <= kl <= 1024) */
+                                     raw vectors (needs gbivf_index_set_refine; k <= kl <= 1024). FP32:
+                                     sequential sums over the 8 blocks of 16 dimensions, then the 8
+                                     partial sums in block order */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -178,6 +180,12 @@ int gbivf_index_autotune(gbivf_index *ix, const float *d_queries, int nq, int k,
  * Waits for that search to finish. No counterpart in the reference, which
  * prints gettimeofday deltas (sequential/ivf_pq/ivf_search.cpp:105-111). */
 int gbivf_last_stage_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms);
+
+/* The same with the scan split in two: the scan kernel (tables, ADC, top-k)
+ * and the finalize kernel (ordering, the precision form's exact re-score,
+ * RERANK or the refinement re-rank). scan_ms + finalize_ms is the scan time
+ * of gbivf_last_stage_ms. */
+int gbivf_last_stages_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms, float *finalize_ms);
 
 /* The coarse stage alone: knn_full(2, nq, C, d, w, coa, queries, ...)
  * (sequential/ivf_pq/ivf_search.cpp:37-38): the w nearest lists per query,

@@ -129,7 +129,8 @@ struct gbivf_index {
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
     // precision form of the scan: per-list table terms (C x m x 256), hand-off lists
     DBuf term2, w_clist;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // stage events (GBIVF_PROFILE)
+    // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_valid = false;
 };
 
@@ -323,7 +324,7 @@ int coarse_batch(int nq, int C) {
 }
 
 // the persistent register-codebook kernel where it applies, else the general one
-int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
+int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nullptr) {
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
     const bool mixed = a.flags & SCAN_MIXED;
@@ -357,9 +358,10 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st) {
             CK(ix->w_clist.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
             a.cand_list = ix->w_clist.as<int32_t>();
         }
-        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st));
+        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st, mid));
     } else {
         CK(launch_scan(ix->dx, a, st));
+        if (mid) CK(cudaEventRecord(mid, st));  // one kernel: no separate finalize
     }
     return GBIVF_OK;
 }
@@ -635,7 +637,7 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.out_off = d_off;
     if (prof) CK(cudaEventRecord(ix->ev[1], st));
     {
-        int rs = run_scan(ix, a, st);
+        int rs = run_scan(ix, a, st, prof ? ix->ev[3] : nullptr);
         if (rs) return rs;
     }
     if (prof) {
@@ -837,6 +839,21 @@ int gbivf_last_stage_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms) {
     CK(cudaEventElapsedTime(&b, ix->ev[1], ix->ev[2]));
     if (coarse_ms) *coarse_ms = a;
     if (scan_ms) *scan_ms = b;
+    return GBIVF_OK;
+}
+
+int gbivf_last_stages_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms, float* finalize_ms) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (!ix->ev_valid) return fail(GBIVF_ERR_INVALID, "no search with GBIVF_PROFILE since the last one without");
+    DeviceGuard g(ix->device);
+    CK(cudaEventSynchronize(ix->ev[2]));
+    float a = 0, b = 0, c = 0;
+    CK(cudaEventElapsedTime(&a, ix->ev[0], ix->ev[1]));
+    CK(cudaEventElapsedTime(&b, ix->ev[1], ix->ev[3]));
+    CK(cudaEventElapsedTime(&c, ix->ev[3], ix->ev[2]));
+    if (coarse_ms) *coarse_ms = a;
+    if (scan_ms) *scan_ms = b;
+    if (finalize_ms) *finalize_ms = c;
     return GBIVF_OK;
 }
 

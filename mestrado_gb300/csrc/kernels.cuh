@@ -94,9 +94,10 @@ cudaError_t launch_coarse_select(const float* dist, int nq, int C, int w, int32_
 cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
 
 // persistent register-codebook scan (d = 128, ks = 256, m in {4, 8, 16},
-// k or kl <= 1024); returns cudaErrorNotSupported when not applicable
+// k or kl <= 1024) and its finalize kernel; `mid`, when given, is recorded between
+// the two; returns cudaErrorNotSupported when not applicable
 cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads,
-                                   cudaStream_t st);
+                                   cudaStream_t st, cudaEvent_t mid = nullptr);
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);

@@ -79,6 +79,25 @@ __device__ __forceinline__ float adc_sum16(uint2 v, const __half* T) {
 __device__ __forceinline__ float adc_sum16(uint4 v, const __half* T) {
     return adc4h(adc4h(adc4h(adc4h(0.0f, v.x, T), v.y, T + 1024), v.z, T + 2048), v.w, T + 3072) * 4.0f;
 }
+// The ADC loop reads code rows in 16-byte groups (G = 16 / M rows: 4 at m = 4, 2 at m = 8, 1 at
+// m = 16), so that a thread's bounds checks, filter vote and loop control are paid once per group,
+// not once per row. List starts and the end of the code array are padded to whole groups.
+__device__ __forceinline__ uint4 load_group(const uint8_t* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+
+// ADC distance of row r (0 <= r < 16 / M) of a group
+template <int M, bool MIXED>
+__device__ __forceinline__ float group_row_dist(const uint4& c, int r, const float* T, const __half* T16) {
+    if constexpr (M == 16) {
+        return MIXED ? adc_sum16(c, T16) : adc_sum(c, T);
+    } else if constexpr (M == 8) {
+        const uint2 v = r == 0 ? make_uint2(c.x, c.y) : make_uint2(c.z, c.w);
+        return MIXED ? adc_sum16(v, T16) : adc_sum(v, T);
+    } else {
+        const uint32_t v = r == 0 ? c.x : (r == 1 ? c.y : (r == 2 ? c.z : c.w));
+        return MIXED ? adc_sum16(v, T16) : adc_sum(v, T);
+    }
+}
+
 __device__ __forceinline__ unsigned short f16_sat(float x) {
     unsigned short h;
     asm("cvt.rn.satfinite.f16.f32 %0, %1;" : "=h"(h) : "f"(x));
@@ -89,9 +108,11 @@ template <int M, bool DIRECT, int NT, bool MIXED = false>
 __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix, ScanArgs a, ScanSmem L, int kcap) {
     constexpr int D = 128, KS = 256, DS = D / M, E = M * KS / NT;
     constexpr int TPS = NT / M;  // threads per sub-quantizer
-    constexpr int U = M >= 16 ? 2 : 4;
-    using CT = typename CodeRow<M>::T;
+    constexpr int G = 16 / M;              // code rows per 16-byte group
+    constexpr int U = M == 4 ? 1 : 2;      // groups per thread per chunk
+    constexpr int CH = NT * U * G;         // code rows per chunk
     static_assert(E * NT == M * KS && E * TPS == KS, "entries must divide evenly");
+    static_assert(G * M == 16, "m must be 4, 8 or 16");
     extern __shared__ __align__(16) unsigned char smem[];
     u64* best = reinterpret_cast<u64*>(smem + L.off_best);
     u64* tmp = reinterpret_cast<u64*>(smem + L.off_tmp);
@@ -195,17 +216,17 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
 
         // precision form: the next probe's table terms and first code chunk load during this probe
         // (its table build is a few adds, too short to hide an HBM round trip)
-        CT pre[MIXED ? U : 1];
+        uint4 pre[MIXED ? U : 1];
         float t2n[MIXED ? E : 1];
         auto load_probe = [&](int jj) {
             if constexpr (MIXED) {
                 const int ll = jj < wq ? plist[jj] : -1;
-                const int ln = ll >= 0 ? __ldg(ix.list_len + ll) : 0;
+                const int ngp = ll >= 0 ? (__ldg(ix.list_len + ll) + G - 1) / G : 0;
                 const uint8_t* cp = ix.codes + (ll >= 0 ? __ldg(ix.list_beg + ll) : 0) * (int64_t)M;
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int i = u * NT + tid;
-                    pre[u] = i < ln ? load_row<M>(cp + (int64_t)i * M) : CT{};
+                    const int g = u * NT + tid;
+                    pre[u] = g < ngp ? load_group(cp + (int64_t)g * 16) : make_uint4(0, 0, 0, 0);
                 }
                 const float* t2 = a.term2 + ((int64_t)(ll >= 0 ? ll : 0) * M + my_s) * KS + my_c0;
                 if constexpr (E % 4 == 0) {
@@ -244,7 +265,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     for (int e = tid; e < nr * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
                 __syncthreads();
             }
-            CT cur[U];
+            uint4 cur[U];
             float t2c[MIXED ? E : 1];
             if constexpr (MIXED) {
 #pragma unroll
@@ -256,13 +277,14 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             const int l = plist[j];
             if (l < 0) continue;
             const int len = __ldg(ix.list_len + l);
+            const int ng = (len + G - 1) / G;  // 16-byte groups of code rows
             const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
             if constexpr (!MIXED) {
                 // first chunk of codes in flight during the table build
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int i = u * NT + tid;
-                    cur[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+                    const int g = u * NT + tid;
+                    cur[u] = g < ng ? load_group(codes + (int64_t)g * 16) : make_uint4(0, 0, 0, 0);
                 }
             }
             float* table = tables + (j & 1) * (M * KS);
@@ -375,39 +397,49 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             float td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
             uint32_t tp = key_payload(tk);
             // two chunk buffers used in turn (unrolled by two, so nothing is copied between them)
-            auto load_chunk = [&](CT(&dst)[U], int i0) {
+            auto load_chunk = [&](uint4(&dst)[U], int g0) {
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int i = i0 + u * NT + tid;
-                    dst[u] = i < len ? load_row<M>(codes + (int64_t)i * M) : CT{};
+                    const int g = g0 + u * NT + tid;
+                    dst[u] = g < ng ? load_group(codes + (int64_t)g * 16) : make_uint4(0, 0, 0, 0);
                 }
             };
-            auto scan_chunk = [&](const CT(&c)[U], int i0) {
+            auto scan_chunk = [&](const uint4(&c)[U], int g0) {
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int iw = i0 + u * NT + (tid & ~31);
-                    if (iw < len) {
-                        const int i = i0 + u * NT + tid;
-                        const float dist = MIXED ? adc_sum16(c[u], table16) : adc_sum(c[u], table);
-                        const uint32_t pos = pos0 + (uint32_t)i;
-                        const bool pass = i < len && (dist < td || (dist == td && pos < tp));
-                        topk_push(s, make_key(dist, pos), pass);
+                    const int gw = g0 + u * NT + (tid & ~31);
+                    if (gw < ng) {
+                        const int i0 = (g0 + u * NT + tid) * G;  // first row of this thread's group
+                        float dist[G];
+                        bool pass[G], any = false;
+#pragma unroll
+                        for (int r = 0; r < G; r++) {
+                            dist[r] = group_row_dist<M, MIXED>(c[u], r, table, table16);
+                            const uint32_t pos = pos0 + (uint32_t)(i0 + r);
+                            pass[r] = i0 + r < len && (dist[r] < td || (dist[r] == td && pos < tp));
+                            any |= pass[r];
+                        }
+                        if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+                            for (int r = 0; r < G; r++)
+                                topk_push(s, make_key(dist[r], pos0 + (uint32_t)(i0 + r)), pass[r]);
+                        }
                     }
                 }
                 if (!fits) {
-                    topk_round_end(s, NT * U);
+                    topk_round_end(s, CH);
                     tk = *s.thresh;
                     td = tk == KEY_MAX ? __int_as_float(0x7f800000) : key_dist(tk);
                     tp = key_payload(tk);
                 }
             };
-            for (int i0 = 0; i0 < len; i0 += 2 * NT * U) {
-                CT nxt[U];
-                load_chunk(nxt, i0 + NT * U);
-                scan_chunk(cur, i0);
-                if (i0 + NT * U >= len) break;
-                load_chunk(cur, i0 + 2 * NT * U);
-                scan_chunk(nxt, i0 + NT * U);
+            for (int g0 = 0; g0 < ng; g0 += 2 * NT * U) {
+                uint4 nxt[U];
+                load_chunk(nxt, g0 + NT * U);
+                scan_chunk(cur, g0);
+                if (g0 + NT * U >= ng) break;
+                load_chunk(cur, g0 + 2 * NT * U);
+                scan_chunk(nxt, g0 + NT * U);
             }
         }
         // final merge; hand the unsorted best set (keys and base ids) over
@@ -444,7 +476,11 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
 
 // Per query (one CTA): sort the hand-off set, then write it, or re-rank it by
 // exact L2 (ivf_search.cpp:113-134) and write the k best.
+// finalize threads per query: 128 (sort, RERANK by raw vectors, the precision form's re-score:
+// one candidate per thread), 512 for the refinement re-rank of the exact form (eight lanes per
+// candidate)
 constexpr int FIN_NT = 128;
+constexpr int FIN_NT_BIG = 512;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -527,38 +563,59 @@ __device__ __forceinline__ float exact_adc(const DevIndex& ix, const float* xq, 
     return dist;
 }
 
-// Distance from the query to the refined reconstruction y_l + c1(codes) + c2(codes2) of one code
-// row (refinement codes of the residual error), FP32 in dimension order. d = 128.
-__device__ inline float refined_dist(const DevIndex& ix, const float* xq, int l, int64_t row) {
-    const int m = ix.m, ds = ix.ds, m2 = ix.m2, ds2 = ix.ds2;
-    const uint8_t* c1 = ix.codes + row * m;
-    const uint8_t* c2 = ix.codes2 + row * m2;
-    const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128);
-    float dist = 0.0f;
-#pragma unroll 4
-    for (int t4 = 0; t4 < 32; t4++) {
-        const int t = 4 * t4, s = t / ds, s2 = t / ds2;
-        const float4 y = __ldg(y4 + t4);
-        const float4 a = __ldg(reinterpret_cast<const float4*>(ix.pq + ((int64_t)s * 256 + c1[s]) * ds + (t - s * ds)));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(ix.pq2 + ((int64_t)s2 * 256 + c2[s2]) * ds2 + (t - s2 * ds2)));
-        const float e0 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t], y.x), a.x), b.x);
-        const float e1 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 1], y.y), a.y), b.y);
-        const float e2 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 2], y.z), a.z), b.z);
-        const float e3 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 3], y.w), a.w), b.w);
-        dist = __fadd_rn(dist, __fmul_rn(e0, e0));
-        dist = __fadd_rn(dist, __fmul_rn(e1, e1));
-        dist = __fadd_rn(dist, __fmul_rn(e2, e2));
-        dist = __fadd_rn(dist, __fmul_rn(e3, e3));
+// Refinement re-rank of candidates 0 .. n-1 (in ADC order; ids[c] is the hand-off slot of
+// candidate c): keys[c] = (||x - y_l - c1(codes) - c2(codes2)||^2, c). FP32; eight lanes take one
+// candidate, lane b the 16 dimensions 16b .. 16b+15: e_t = ((x_t - y_t) - c1_t) - c2_t, the lane's
+// partial sum of e_t^2 in dimension order from 0, then the eight partials summed in b order from 0.
+// (The refinement codes have no counterpart in the reference; this order is the definition.)
+template <int M>
+__device__ __forceinline__ void refine_rerank(const DevIndex& ix, const ScanArgs& a, int64_t hb, const float* xq,
+                                              const int32_t* ids, u64* keys, int n) {
+    constexpr int DS = 128 / M;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = lane & 7, grp = lane >> 3, t0 = 16 * b;
+    const int m2 = ix.m2, sh2 = __ffs(ix.ds2) - 1;  // ds2 = 128 / m2, a power of two >= 4
+    for (int c0 = warp * 4; c0 < n; c0 += (blockDim.x >> 5) * 4) {  // warp-uniform bound
+        const int c = c0 + grp;
+        float p = 0.0f;
+        if (c < n) {
+            const int64_t slot = hb + ids[c];
+            const int64_t row = a.cand_id[slot];
+            const int l = a.cand_list[slot];
+            const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128 + t0);
+            const uint8_t* c1 = ix.codes + row * M;
+            const uint8_t* c2 = ix.codes2 + row * m2;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int t = t0 + 4 * v, s = t / DS, s2 = t >> sh2;
+                const float4 y = __ldg(y4 + v);
+                const float4 av = __ldg(reinterpret_cast<const float4*>(ix.pq + ((int64_t)s * 256 + c1[s]) * DS + (t - s * DS)));
+                const float4 bv = __ldg(reinterpret_cast<const float4*>(
+                    ix.pq2 + (((int64_t)s2 * 256 + c2[s2]) << sh2) + (t - (s2 << sh2))));
+                const float e0 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t], y.x), av.x), bv.x);
+                const float e1 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 1], y.y), av.y), bv.y);
+                const float e2 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 2], y.z), av.z), bv.z);
+                const float e3 = __fsub_rn(__fsub_rn(__fsub_rn(xq[t + 3], y.w), av.w), bv.w);
+                p = __fadd_rn(p, __fmul_rn(e0, e0));
+                p = __fadd_rn(p, __fmul_rn(e1, e1));
+                p = __fadd_rn(p, __fmul_rn(e2, e2));
+                p = __fadd_rn(p, __fmul_rn(e3, e3));
+            }
+        }
+        float dist = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 8; t++) dist = __fadd_rn(dist, __shfl_sync(0xffffffffu, p, grp * 8 + t));
+        if (c < n && b == 0) keys[c] = make_key(dist, (uint32_t)c);
     }
-    return dist;
 }
 
 // Per query (one CTA): order the hand-off set, then write it, or re-rank it and write the k best.
 // The sort carries the keys and, with them, either base ids (the exact form) or hand-off slots
 // (precision form, refinement re-rank: the slot leads to the candidate's code row and list).
-template <bool MIXED, int M = 8>
-__global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs a) {
+template <bool MIXED, int M, int NT>
+__global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
+    constexpr int FIN_NT = NT;
     const int n2 = a.cand_stride;  // power of two
     u64* keys = reinterpret_cast<u64*>(fsm);
     int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
@@ -622,14 +679,16 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(DevIndex ix, ScanArgs 
     const int d = ix.d;
     int pr = 2;
     while (pr < n) pr <<= 1;
+    if (refine) {
+        // keys[c] for c < n: every lane reads ids[] and keys[] of its own candidate only
+        refine_rerank<M>(ix, a, hb, xq, ids, keys, n);
+        for (int c = n + tid; c < pr; c += FIN_NT) keys[c] = KEY_MAX;
+    } else
     for (int c = tid; c < pr; c += FIN_NT) {
         u64 key = KEY_MAX;
         if (c < n) {
             float dist;
-            if (refine) {
-                const int64_t slot = hb + ids[c];
-                dist = refined_dist(ix, xq, a.cand_list[slot], a.cand_id[slot]);
-            } else {
+            {
                 const int32_t id = base_id(c);
                 const float4* v4 = reinterpret_cast<const float4*>(ix.base + (int64_t)id * d);
                 float dot = 0.0f;
@@ -676,7 +735,7 @@ int scan_persistent_stride(const ScanArgs& a) {
 }
 
 template <int M, bool DIRECT, int NT, bool MIXED = false>
-static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
+static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid) {
     const int kcap = scan_persistent_stride(a);
     if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
     if (MIXED && (!a.term2 || !a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
@@ -695,39 +754,47 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
     kern<<<grid, NT, L.total, st>>>(ix, a, L, kcap);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const size_t fsm = (size_t)kcap * (sizeof(u64) + sizeof(int32_t)) + sizeof(float) * 128;
-    auto fin = finalize_kernel<MIXED, M>;
+    if (mid && (e = cudaEventRecord(mid, st)) != cudaSuccess) return e;
+    const size_t fsm = (size_t)a.cand_stride * 12 + 512;  // keys, ids, the query
+    const bool big = !MIXED && (a.flags & SCAN_REFINE);
+    void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
+    if constexpr (!MIXED)
+        if (big) fin = finalize_kernel<false, M, FIN_NT_BIG>;
     if (fsm > 48 * 1024) {
         e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
         if (e != cudaSuccess) return e;
     }
-    fin<<<a.nq, FIN_NT, fsm, st>>>(ix, a);
+    fin<<<a.nq, big ? FIN_NT_BIG : FIN_NT, fsm, st>>>(ix, a);
     return cudaGetLastError();
 }
 
 template <int NT>
-static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st) {
+static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid) {
     const bool direct = a.flags & SCAN_TABLE_DIRECT;
     if (a.flags & SCAN_MIXED) {  // the precision form: expansion tables only
         if (direct) return cudaErrorNotSupported;
         switch (ix.m) {
-            case 4: return launch_sp<4, false, NT, true>(ix, a, num_sms, st);
-            case 8: return launch_sp<8, false, NT, true>(ix, a, num_sms, st);
-            default: return launch_sp<16, false, NT, true>(ix, a, num_sms, st);
+            case 4: return launch_sp<4, false, NT, true>(ix, a, num_sms, st, mid);
+            case 8: return launch_sp<8, false, NT, true>(ix, a, num_sms, st, mid);
+            default: return launch_sp<16, false, NT, true>(ix, a, num_sms, st, mid);
         }
     }
     switch (ix.m) {
-        case 4: return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st) : launch_sp<4, false, NT>(ix, a, num_sms, st);
-        case 8: return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st) : launch_sp<8, false, NT>(ix, a, num_sms, st);
+        case 4:
+            return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st, mid) : launch_sp<4, false, NT>(ix, a, num_sms, st, mid);
+        case 8:
+            return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st, mid) : launch_sp<8, false, NT>(ix, a, num_sms, st, mid);
         default:
-            return direct ? launch_sp<16, true, NT>(ix, a, num_sms, st) : launch_sp<16, false, NT>(ix, a, num_sms, st);
+            return direct ? launch_sp<16, true, NT>(ix, a, num_sms, st, mid)
+                          : launch_sp<16, false, NT>(ix, a, num_sms, st, mid);
     }
 }
 
-cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads, cudaStream_t st) {
+cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads, cudaStream_t st,
+                                   cudaEvent_t mid) {
     if (a.nq <= 0) return cudaSuccess;
     if (!scan_persistent_supported(ix, a)) return cudaErrorNotSupported;
-    return threads == 1024 ? launch_sp_nt<1024>(ix, a, num_sms, st) : launch_sp_nt<512>(ix, a, num_sms, st);
+    return threads == 1024 ? launch_sp_nt<1024>(ix, a, num_sms, st, mid) : launch_sp_nt<512>(ix, a, num_sms, st, mid);
 }
 
 }  // namespace gbivf

@@ -181,6 +181,12 @@ class GpuIndex:
         check(self.lib.gbivf_last_stage_ms(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def last_stages_ms(self):
+        """(coarse_ms, scan_kernel_ms, finalize_ms) of the last search made with profile=True."""
+        a, b, c = C.c_float(), C.c_float(), C.c_float()
+        check(self.lib.gbivf_last_stages_ms(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def coarse_assign(self, queries, w, mixed=False, stats=False, full=False):
         """knn_full over the coarse centroids: (coaidx, coadis) nq x w. With
         mixed=True the tensor-core form runs, with full=True the full-block

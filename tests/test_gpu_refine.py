@@ -1,7 +1,8 @@
 """Refinement-code re-rank (GB300): the kl ADC candidates re-ranked by the
 distance to their refined reconstruction y + c1(codes) + c2(codes2). Checked
-against a numpy restatement (FP32, the kernel's operation order) applied to
-the oracle's keyed ADC top-kl."""
+against a numpy restatement (FP32 in the defined order: sequential partial
+sums over the eight blocks of 16 dimensions, then the partials summed in
+block order) applied to the oracle's keyed ADC top-kl."""
 import numpy as np
 import pytest
 
@@ -24,13 +25,16 @@ def refined_reference(ix, q, adc_ids, k):
         rows = row_of[cand]
         lists = list_of[rows]
         dist = np.zeros(len(cand), np.float32)
-        for t in range(128):
-            s, s2 = t // ds, t // ds2
-            y = ix.coa[lists, t]
-            a = ix.pq[s, ix.codes[rows, s], t - s * ds]
-            b = ix.pq2[s2, ix.codes2[rows, s2], t - s2 * ds2]
-            e = ((np.float32(q[qi, t]) - y) - a) - b
-            dist = dist + e * e
+        for blk in range(8):
+            part = np.zeros(len(cand), np.float32)
+            for t in range(16 * blk, 16 * blk + 16):
+                s, s2 = t // ds, t // ds2
+                y = ix.coa[lists, t]
+                a = ix.pq[s, ix.codes[rows, s], t - s * ds]
+                b = ix.pq2[s2, ix.codes2[rows, s2], t - s2 * ds2]
+                e = ((np.float32(q[qi, t]) - y) - a) - b
+                part = part + e * e
+            dist = dist + part
         order = np.lexsort((np.arange(len(cand)), dist))[:k]
         out_ids.append(cand[order])
         out_dis.append(dist[order])
