@@ -300,6 +300,14 @@ int gbivf_pq_error(const float *d_x, int64_t n, int d, const int32_t *d_coarse, 
 int gbivf_pq_encode(const float *d_x, int64_t n, int d, const int32_t *d_coarse, const float *d_coa,
                     int m, const float *d_pq, uint8_t *d_codes, void *stream);
 
+/* Self-test of the bounded device-side waits (no counterpart in the reference):
+ * runs one CTA of the tensor-core coarse product with its first centroid-tile
+ * copy withheld, so that the wait for it runs out (after about 2 s of the
+ * global timer); the kernel must stop, report it (timed_out = 1) and leave
+ * the context usable, which a second, normal run checks (clean_ok = 1).
+ * stalled_ms: the stalled launch's duration. Nothing faults. */
+int gbivf_selftest_wait_timeout(int device, int *timed_out, float *stalled_ms, int *clean_ok);
+
 #ifdef __cplusplus
 }
 #endif

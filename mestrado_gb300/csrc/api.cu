@@ -1394,6 +1394,58 @@ int gbivf_pq_error(const float* d_x, int64_t n, int d, const int32_t* d_coarse, 
     return GBIVF_OK;
 }
 
+int gbivf_selftest_wait_timeout(int device, int* timed_out, float* stalled_ms, int* clean_ok) {
+    if (!timed_out || !stalled_ms || !clean_ok) return fail(GBIVF_ERR_INVALID, "NULL output");
+    *timed_out = 0;
+    *stalled_ms = 0.0f;
+    *clean_ok = 0;
+    DeviceGuard g(device);
+    if (!g.ok) return fail(GBIVF_ERR_INVALID, "device %d", device);
+    // one CTA of the persistent tensor-core product: 256 zero queries x 128 zero centroids
+    const int nq = 256, C = 128;
+    struct Bufs {
+        void* p[6] = {};
+        cudaStream_t st = nullptr;
+        cudaEvent_t e[2] = {};
+        ~Bufs() {
+            for (void* x : p) if (x) cudaFree(x);
+            for (cudaEvent_t x : e) if (x) cudaEventDestroy(x);
+            if (st) cudaStreamDestroy(st);
+        }
+    } b;
+    const size_t bytes[6] = {coarse_gemm_qtile_bytes(nq), (size_t)C * 128 * 2 * 2, sizeof(double) * nq,
+                             sizeof(float) * C, sizeof(float) * nq * C, sizeof(int)};
+    for (int i = 0; i < 6; i++) {
+        CK(cudaMalloc(&b.p[i], bytes[i]));
+        CK(cudaMemset(b.p[i], 0, bytes[i]));
+    }
+    CK(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b.e[0]));
+    CK(cudaEventCreate(&b.e[1]));
+    int* d_err = static_cast<int*>(b.p[5]);
+    auto run = [&](bool stall, int* h_err) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), b.st);
+        if (e == cudaSuccess) e = cudaEventRecord(b.e[0], b.st);
+        if (e == cudaSuccess)
+            e = launch_coarse_gemm_store(static_cast<uint8_t*>(b.p[0]), static_cast<uint8_t*>(b.p[1]), nq, C,
+                                         static_cast<double*>(b.p[2]), static_cast<float*>(b.p[3]),
+                                         static_cast<float*>(b.p[4]), C, 1, d_err, b.st, stall);
+        if (e == cudaSuccess) e = cudaEventRecord(b.e[1], b.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, b.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b.st);
+        return e;
+    };
+    int h_err = 0;
+    CK(run(true, &h_err));
+    *timed_out = h_err != 0;
+    CK(cudaEventElapsedTime(stalled_ms, b.e[0], b.e[1]));
+    // the context must still run work: the same product without the stall
+    h_err = 1;
+    CK(run(false, &h_err));
+    *clean_ok = h_err == 0;
+    return GBIVF_OK;
+}
+
 int gbivf_pq_encode(const float* d_x, int64_t n, int d, const int32_t* d_coarse, const float* d_coa, int m,
                     const float* d_pq, uint8_t* d_codes, void* stream) {
     if (!d_x || !d_pq || !d_codes || n < 0 || m <= 0 || d % m || (d_coarse && !d_coa))

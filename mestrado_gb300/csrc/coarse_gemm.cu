@@ -63,6 +63,9 @@ struct PgArgs {
     const float* colK = nullptr;   // nct * 128: MIXED_EPS_REL ||c|| / 2, 0 past C
     float cn_max = 0.0f, clen_max = 0.0f;
     int* err = nullptr;
+    // self-test of the bounded waits: the first centroid-tile copy is never issued, so the MMA
+    // warp's wait for it runs out; the kernel must report the error and leave the context usable
+    bool stall_copy = false;
 };
 
 enum PgMode { PG_STORE = 0, PG_CHUNKMIN = 1, PG_FILTER = 2, PG_ARGMIN = 3 };
@@ -216,6 +219,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1) coarse_gemm_kernel(PgArgs p) {
                         ok = false;
                         break;
                     }
+                    if (p.stall_copy && tc == 0) continue;  // self-test only: b_full[0] never completes
                     const uint32_t bbytes = p.hi_only ? B_HALF_BYTES : B_TILE_BYTES;
                     mbar_expect_tx(&b_full[s], bbytes);
                     bulk_load(sB + s * B_TILE_BYTES, p.ctiles + (int64_t)t * B_TILE_BYTES, bbytes, &b_full[s]);
@@ -446,9 +450,10 @@ static cudaError_t launch_pg(PgArgs& p, int mode, int num_sms, cudaStream_t st) 
 
 cudaError_t launch_coarse_gemm_store(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
                                      const double* qnorm, const float* cnorm, float* out, int64_t ld, int num_sms,
-                                     int* err, cudaStream_t st) {
+                                     int* err, cudaStream_t st, bool stall_copy) {
     if (!out || ld < C) return cudaErrorInvalidValue;
     PgArgs p;
+    p.stall_copy = stall_copy;
     p.qtiles = qtiles;
     p.ctiles = ctiles;
     p.nq = nq;

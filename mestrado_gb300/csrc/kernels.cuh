@@ -172,7 +172,7 @@ size_t coarse_gemm_col_floats(int C);
 // approximate distances nq x C (row stride ld)
 cudaError_t launch_coarse_gemm_store(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
                                      const double* qnorm, const float* cnorm, float* out, int64_t ld, int num_sms,
-                                     int* err, cudaStream_t st);
+                                     int* err, cudaStream_t st, bool stall_copy = false);
 // per query and 32 centroids, about the smallest upper bound approx + eps: nq x C/32 (C % 32 == 0)
 cudaError_t launch_coarse_gemm_chunkmin(const uint8_t* qtiles, const uint8_t* ctiles, int nq, int C,
                                         const double* qnorm, const float* cnorm, const float* colG,

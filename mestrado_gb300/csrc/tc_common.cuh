@@ -14,7 +14,17 @@ constexpr int B_HALF_BYTES = MM_N * MM_K * 2;      // 32 KB: one of c_hi / c_lo
 constexpr int B_TILE_BYTES = 2 * B_HALF_BYTES;     // c_hi tile then c_lo tile
 constexpr uint32_t CORE_LBO = 128;                 // next core matrix along K
 constexpr uint32_t CORE_SBO = 2048;                // next 8-row group
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
+// Every mbarrier wait is bounded: it gives up after WAIT_NS nanoseconds of the global timer
+// (try_wait may suspend the thread for an implementation-defined time per poll, so a poll count
+// alone bounds nothing in time), or after WAIT_LIMIT polls as a backstop.
+constexpr uint32_t WAIT_LIMIT = 1u << 28;
+constexpr uint64_t WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // BF16 x BF16 -> F32, K-major A and B, M = 128, N = 128 (kind::f16 descriptor:
 // D format bits 4-5, A/B formats bits 7-9 / 10-12, N>>3 bits 17-22, M>>4 bits 24-28)
@@ -33,8 +43,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+// wait for the phase with the given parity; false once *abort is set (abort may be NULL) or the
+// wait runs out (WAIT_NS, WAIT_LIMIT)
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t phase, volatile int* abort) {
     const uint32_t a = smem_addr(bar);
+    uint64_t t0 = 0;
     for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
         uint32_t done;
         asm volatile(
@@ -43,9 +56,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
             : "r"(a), "r"(phase)
             : "memory");
         if (done) return true;
+        if ((i & 7) == 7) {
+            if (abort && *abort) return false;
+            const uint64_t now = globaltimer_ns();
+            if (t0 == 0) t0 = now;
+            else if (now - t0 > WAIT_NS) return false;
+        }
     }
     return false;
 }
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) { return mbar_wait_or_abort(bar, phase, nullptr); }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -54,23 +75,6 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __host__ __device__ inline uint32_t tile_offset(int row, int k) {
     return (uint32_t)(row >> 3) * CORE_SBO + (uint32_t)(k >> 3) * CORE_LBO + (uint32_t)(row & 7) * 16u +
            (uint32_t)(k & 7) * 2u;
-}
-
-// wait for the phase with the given parity; false after WAIT_LIMIT polls or
-// once *abort is set (abort may be NULL)
-__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t phase, volatile int* abort) {
-    const uint32_t a = smem_addr(bar);
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(phase)
-            : "memory");
-        if (done) return true;
-        if (abort && (i & 63) == 63 && *abort) return false;
-    }
-    return false;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
