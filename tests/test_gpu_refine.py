@@ -41,7 +41,7 @@ def refined_reference(ix, q, adc_ids, k):
     return np.array(out_ids), np.array(out_dis)
 
 
-def built_index(m2=8):
+def built_index(m2=8, m=8):
     from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
     from mestrado_gb300.synth import Mixture
 
@@ -49,7 +49,7 @@ def built_index(m2=8):
     base = g.generate(60000, stream_id=1)
     train = g.generate(30000, stream_id=2)
     q = g.generate(40, stream_id=3).cpu().numpy()
-    ix = build_index_gpu(base, train, coarsek=128, m=8, niter=5, seed=4, m2=m2)
+    ix = build_index_gpu(base, train, coarsek=128, m=m, niter=5, seed=4, m2=m2)
     return ix, q, base.cpu().numpy()
 
 
@@ -73,6 +73,24 @@ def test_refined_rerank_matches_reference():
     err_adc = np.abs(adc_dis - ((q[:, None, :].astype(np.float64) - base[adc_top]) ** 2).sum(-1)).mean()
     print(f"mean |refined - true| {err_refined:.1f}, mean |adc - true| {err_adc:.1f}")
     assert err_refined < err_adc
+    gi.close()
+
+
+@pytest.mark.parametrize("m,m2", [(16, 16), (4, 16), (16, 4)])
+def test_refined_rerank_other_shapes(m, m2):
+    """Sub-vector lengths other than 16: a lane's 16 dimensions span two sub-quantizers (ds = 8)
+    or half of one (ds = 32), for the PQ codes and the refinement codes alike."""
+    from mestrado_gb300.engine import GpuIndex
+
+    ix, q, _ = built_index(m2=m2, m=m)
+    gi = GpuIndex(ix)
+    k, kl, w = 10, 100, 12
+    adc_ids, _ = oracle.ivfpq_search(ix, q, k=kl, kl=kl, w=w, rerank=False, ties=oracle.TIES_KEYED)
+    r_ids, r_dis = refined_reference(ix, q, adc_ids, k)
+    for mixed in (False, True):
+        ids, dis = gi.search(q, k, w, kl=kl, refine=True, mixed_scan=mixed, mixed_coarse=mixed)
+        np.testing.assert_array_equal(ids, r_ids)
+        np.testing.assert_array_equal(dis.view(np.uint32), r_dis.view(np.uint32))
     gi.close()
 
 
