@@ -128,7 +128,7 @@ struct gbivf_index {
     // filtered coarse stage (large C): per-query bounds, counters, candidate slots, GEMM survivors
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
     // precision form of the scan: per-list table terms (C x m x 256), hand-off lists
-    DBuf term2, w_clist;
+    DBuf w_clist;
     // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_valid = false;
@@ -154,7 +154,7 @@ void free_index(gbivf_index* ix) {
     for (DBuf* b : {&ix->base, &ix->base_norm, &ix->w_q, &ix->w_qn, &ix->w_coaidx, &ix->w_coadis,
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
-                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->term2, &ix->w_clist,
+                    &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->w_clist,
                     &ix->pq2, &ix->codes2})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
@@ -329,13 +329,6 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
     a.queue = ix->w_queue.as<int>();
     const bool mixed = a.flags & SCAN_MIXED;
     if (mixed) {
-        // precision form: per-list table terms, built once per index
-        if (!ix->term2.p) {
-            const DevIndex& dx = ix->dx;
-            CK(ix->term2.ensure(sizeof(float) * (size_t)dx.C * dx.m * dx.ks));
-            CK(launch_term2(dx, ix->term2.as<float>(), st));
-        }
-        a.term2 = ix->term2.as<float>();
         a.sel_mult = GBIVF_MIXED_SCAN_ALPHA;
         a.sel_cap = 4096;
         if (!scan_persistent_supported(ix->dx, a))

@@ -25,7 +25,7 @@
 
 namespace gbivf {
 
-constexpr int TOPK_WORK_BYTES = 256 * 4 + 8 * 4 + 4 * 8;  // histogram, ints, u64 slots
+constexpr int TOPK_WORK_BYTES = 2 * 256 * 4 + 16 * 4 + 4 * 8;  // two histograms, ints, u64 slots
 
 struct TopKSmem {
     u64* best;    // [kcap] best set (unordered until topk_finish), nbest valid
@@ -36,9 +36,11 @@ struct TopKSmem {
     u64* thresh;  // current k-th best key (KEY_MAX until k are known)
     int k, kcap, bcap;
     unsigned char* work;  // TOPK_WORK_BYTES, 8-byte aligned
-    __device__ int* hist() const { return reinterpret_cast<int*>(work); }
-    __device__ int* info() const { return reinterpret_cast<int*>(work + 1024); }
-    __device__ u64* slots() const { return reinterpret_cast<u64*>(work + 1056); }
+    // radix-select pass p uses histogram p & 1 and result ints info() + 8 (p & 1) (info()[4] is
+    // the flush's compaction counter)
+    __device__ int* hist(int p = 0) const { return reinterpret_cast<int*>(work + 1024 * (p & 1)); }
+    __device__ int* info() const { return reinterpret_cast<int*>(work + 2048); }
+    __device__ u64* slots() const { return reinterpret_cast<u64*>(work + 2112); }
 };
 
 __device__ __forceinline__ void topk_init(TopKSmem& s, int k) {
@@ -99,11 +101,13 @@ __device__ inline void bitonic_sort_smem(u64* a, int n) {
 
 // The K-th smallest (1-based) key of A[0..na) u B[0..nb), 1 <= K <= na+nb.
 // Expects slots()[0] == 0 on entry and leaves it 0.
+// Two barriers per 8-bit digit: the passes alternate between two histograms and two result
+// slots, so the next pass's histogram is cleared while this one is filled, and a pass's result
+// is read after the barrier that publishes it without a second barrier before it is reused.
 __device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B, int nb, int K) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
-    int* hist = s.hist();
-    int* info = s.info();
     u64* slot = s.slots();
+    for (int i = tid; i < 256; i += nt) s.hist(0)[i] = 0;  // the first pass's histogram
     const u64 ref = na > 0 ? A[0] : B[0];
     u64 acc = 0;
     for (int i = tid; i < na; i += nt) acc |= A[i] ^ ref;
@@ -120,16 +124,19 @@ __device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B,
     u64 kmask = hib == 63 ? 0ull : (~0ull << (hib + 1));
     u64 kval = ref & kmask;
     int want = K;
-    for (;;) {
+    for (int p = 0;; p++) {
+        int* hist = s.hist(p);
+        int* info = s.info() + 8 * (p & 1);
         const int lob = max(hib - 7, 0);
         const int width = hib - lob + 1;
         const u64 dmask = ((1ull << width) - 1ull);
-        for (int i = tid; i < 256; i += nt) hist[i] = 0;
-        __syncthreads();
         for (int i = tid; i < na; i += nt)
             if ((A[i] & kmask) == kval) atomicAdd(&hist[(A[i] >> lob) & dmask], 1);
         for (int i = tid; i < nb; i += nt)
             if ((B[i] & kmask) == kval) atomicAdd(&hist[(B[i] >> lob) & dmask], 1);
+        // clear the next pass's histogram: its last reader, the previous pass's scan, finished
+        // before that pass's second barrier
+        for (int i = tid; i < 256; i += nt) s.hist(p + 1)[i] = 0;
         __syncthreads();
         if (tid < 32) {
             // lane owns bins 8*lane .. 8*lane+7
@@ -161,7 +168,6 @@ __device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B,
         __syncthreads();
         const int dig = info[0], cnt = info[2];
         want = info[1];
-        __syncthreads();
         kmask |= dmask << lob;
         kval |= (u64)dig << lob;
         if (lob == 0) return kval;  // all 64 bits known

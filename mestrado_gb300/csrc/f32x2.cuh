@@ -34,5 +34,11 @@ __device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+// a * b + c, each pair fused (one rounding): for approximate arithmetic only
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+    f2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
 
 }  // namespace gbivf

@@ -186,35 +186,6 @@ cudaError_t launch_scatter_rows(const uint8_t* src, const int64_t* off, const in
 }
 
 // ---------------------------------------------------------------------------
-// precision form of the scan: per-list table terms
-// ||r_s - c||^2 = ||r_s||^2 - 2 <x_s, c> + (||c||^2 + 2 <y_{l,s}, c>), r = x - y_l;
-// the bracket depends on the list only and is computed once per index
-// ---------------------------------------------------------------------------
-
-__global__ void term2_kernel(const float* __restrict__ coa, const float* __restrict__ pq,
-                             const float* __restrict__ pq_hi, int64_t total, int m, int ks, int ds, int d,
-                             float* __restrict__ out) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= total) return;
-    const int c = (int)(idx % ks);
-    const int s = (int)((idx / ks) % m);
-    const int64_t l = idx / ((int64_t)ks * m);
-    const float* y = coa + l * d + s * ds;
-    const float* cc = pq + ((int64_t)s * ks + c) * ds;
-    float dt = 0.0f;
-    for (int t = 0; t < ds; t++) dt = __fmaf_rn(y[t], cc[t], dt);
-    out[idx] = pq_hi[s * ks + c] + 2.0f * dt;
-}
-
-cudaError_t launch_term2(const DevIndex& ix, float* term2, cudaStream_t st) {
-    const int64_t total = (int64_t)ix.C * ix.m * ix.ks;
-    if (total == 0) return cudaSuccess;
-    term2_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(ix.coa, ix.pq, ix.pq_hi, total, ix.m, ix.ks, ix.ds,
-                                                                  ix.d, term2);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
 // coarse k-min: one CTA per query over its row of C distances
 // ---------------------------------------------------------------------------
 

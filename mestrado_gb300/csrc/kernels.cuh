@@ -60,10 +60,8 @@ struct ScanArgs {
     const int32_t* w_per_q = nullptr;
     const int32_t* k_per_q = nullptr;
     const int64_t* out_off = nullptr;
-    // precision form (SCAN_MIXED): per-list table terms term2[l][s][c] = ||c||^2 + 2 <y_{l,s}, c>
-    // (C x m x 256), the approximate selection size min(sel_mult * k, sel_cap), and the hand-off's
-    // list of each candidate (cand_id then holds its code row)
-    const float* term2 = nullptr;
+    // precision form (SCAN_MIXED): the approximate selection size min(sel_mult * k, sel_cap), and
+    // the hand-off's list of each candidate (cand_id then holds its code row)
     int sel_mult = 1, sel_cap = 0;
     int32_t* cand_list = nullptr;
 };
@@ -107,9 +105,6 @@ cudaError_t launch_id_range(const int32_t* ids, int64_t n, int* range, cudaStrea
 // rows of `width` bytes in list order (list l: rows off[l] .. off[l+1]) -> dst rows beg[l] ..
 cudaError_t launch_scatter_rows(const uint8_t* src, const int64_t* off, const int64_t* beg, int C, int width,
                                 uint8_t* dst, cudaStream_t st);
-
-// precision form of the scan: term2[l][s][c] = ||c||^2 + 2 <y_{l,s}, c> for every list (C x m x ks)
-cudaError_t launch_term2(const DevIndex& ix, float* term2, cudaStream_t st);
 
 // mixed-precision coarse stage (d = 128): BF16 tiles, tcgen05 GEMM, exact re-check
 cudaError_t launch_bf16_tiles(const float* x, int n, int rows_per_tile, uint8_t* out, cudaStream_t st);

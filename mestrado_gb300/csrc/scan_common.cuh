@@ -11,11 +11,13 @@ namespace gbivf {
 
 struct ScanSmem {
     size_t off_best, off_tmp, off_buf, off_thresh, off_table, off_xq, off_r, off_rn, off_prefix,
-        off_plist, off_cand, off_cnt, off_misc, off_work, total;
+        off_plist, off_cand, off_cnt, off_misc, off_work, off_stage, total;
 };
 
-// tables: number of m x ks table buffers; rrows: residual rows held at once
-inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap, int tables = 1, int rrows = 1) {
+// tables: number of m x ks table buffers of table_elem bytes per entry; rrows: residual rows held
+// at once; stage_bytes: staging area for code rows copied ahead (16-byte aligned)
+inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap, int tables = 1, int rrows = 1,
+                                 int table_elem = 4, size_t stage_bytes = 0) {
     ScanSmem L;
     size_t o = 0;
     auto take = [&](size_t bytes, size_t align) {
@@ -28,7 +30,7 @@ inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap
     L.off_tmp = take(sizeof(u64) * kcap, 16);
     L.off_buf = take(sizeof(u64) * bcap, 16);
     L.off_thresh = take(sizeof(u64), 8);
-    L.off_table = take(sizeof(float) * m * ks * tables, 16);
+    L.off_table = take((size_t)table_elem * m * ks * tables, 16);
     L.off_xq = take(sizeof(float) * d, 16);
     L.off_r = take(sizeof(float) * d * rrows, 16);
     L.off_rn = take(sizeof(float) * m * rrows, 16);
@@ -38,6 +40,7 @@ inline ScanSmem scan_smem_layout(int m, int ks, int d, int w, int kcap, int bcap
     L.off_cnt = take(sizeof(int) * 2, 8);
     L.off_misc = take(sizeof(int) * 4, 8);
     L.off_work = take(TOPK_WORK_BYTES, 16);
+    L.off_stage = take(stage_bytes, 16);
     L.total = (o + 15) / 16 * 16;
     return L;
 }

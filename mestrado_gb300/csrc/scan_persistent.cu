@@ -29,6 +29,23 @@ namespace gbivf {
 constexpr int SP_BCAP = 8192;   // candidate buffer (64 KB)
 constexpr int SP_SOFT = 2048;   // flush at a list boundary once this many are buffered
 constexpr int SP_RCH = 16;      // residuals formed per chunk of probes
+// Precision form: the first chunk of each probe's code rows is copied into shared memory
+// SP_AHEAD probes ahead (cp.async, per thread: a thread copies exactly the 16-byte groups it later
+// scans, so it only waits for its own copies, with no barrier), in SP_NS rotating stages. Its
+// probes are short (most probed lists are, and its tables take a few instructions), often shorter
+// than a memory round trip: one probe of lead left the copy exposed at the start of the scan. The
+// exact form loads its first chunk into registers at the start of its (long) table build instead.
+constexpr int SP_AHEAD = 2;
+constexpr int SP_NS = SP_AHEAD + 1;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most n of this thread's committed groups are still in flight
+template <int n>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(n) : "memory"); }
 
 // one code row as a vector load
 template <int M> struct CodeRow;
@@ -98,10 +115,11 @@ __device__ __forceinline__ float group_row_dist(const uint4& c, int r, const flo
     }
 }
 
-__device__ __forceinline__ unsigned short f16_sat(float x) {
-    unsigned short h;
-    asm("cvt.rn.satfinite.f16.f32 %0, %1;" : "=h"(h) : "f"(x));
-    return h;
+// two FP32 values as an FP16 pair (lo in the low half, the lower address), saturating
+__device__ __forceinline__ uint32_t f16x2_sat(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
 }
 
 template <int M, bool DIRECT, int NT, bool MIXED = false>
@@ -111,6 +129,8 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     constexpr int G = 16 / M;              // code rows per 16-byte group
     constexpr int U = M == 4 ? 1 : 2;      // groups per thread per chunk
     constexpr int CH = NT * U * G;         // code rows per chunk
+    // staged groups per thread (precision form; at most 1024 per probe)
+    constexpr int US = !MIXED ? 0 : NT * U > 1024 ? 1024 / NT : U;
     static_assert(E * NT == M * KS && E * TPS == KS, "entries must divide evenly");
     static_assert(G * M == 16, "m must be 4, 8 or 16");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -122,6 +142,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     float* xq = reinterpret_cast<float*>(smem + L.off_xq);
     float* rr = reinterpret_cast<float*>(smem + L.off_r);    // SP_RCH x D residuals
     float* rn = reinterpret_cast<float*>(smem + L.off_rn);   // SP_RCH x M sub-norms
+    uint4* stage = reinterpret_cast<uint4*>(smem + L.off_stage);  // SP_NS x (US x NT) code groups
     uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + L.off_prefix);
     int* plist = reinterpret_cast<int*>(smem + L.off_plist);
     int* cnt = reinterpret_cast<int*>(smem + L.off_cnt);
@@ -135,10 +156,13 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     // this thread's slice of the codebook: sub-quantizer my_s, centroids
     // my_c0 .. my_c0+E-1 (consecutive, so the table row is one vector store)
     const int my_s = tid / TPS, my_c0 = (tid % TPS) * E;
-    // (the precision form builds its tables from per-list terms: no register codebook)
-    constexpr int EC = MIXED ? 1 : E;
-    float cen[EC][DS];
-    float nhi[EC], nlo[EC];
+    // The precision form keeps the same slice as packed pairs of entries (i, i+1) for packed
+    // fused multiply-adds, with ||c||^2 / 4 of each entry (a single entry, E = 1, is paired with
+    // itself and stored once).
+    constexpr int EP = MIXED ? 1 : E, EM = MIXED ? (E + 1) / 2 : 1;
+    float cen[EP][DS];
+    float nhi[EP], nlo[EP];
+    f2_t cen2[EM][DS], cn2[EM];
 #pragma unroll
     for (int i = 0; i < (MIXED ? 0 : E); i++) {
         const int e = my_s * KS + my_c0 + i;
@@ -156,32 +180,50 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             nlo[i] = __ldg(ix.pq_lo + e);
         }
     }
+#pragma unroll
+    for (int i = 0; i < (MIXED ? E : 0); i += 2) {
+        const int e = my_s * KS + my_c0 + i;
+        const float4* s0 = reinterpret_cast<const float4*>(ix.pq + (int64_t)e * DS);
+        const int e1 = i + 1 < E ? e + 1 : e;
+        const float4* s1 = reinterpret_cast<const float4*>(ix.pq + (int64_t)e1 * DS);
+#pragma unroll
+        for (int v = 0; v < DS / 4; v++) {
+            const float4 x = __ldg(s0 + v), y = __ldg(s1 + v);
+            cen2[i / 2][4 * v] = f2_pack(x.x, y.x);
+            cen2[i / 2][4 * v + 1] = f2_pack(x.y, y.y);
+            cen2[i / 2][4 * v + 2] = f2_pack(x.z, y.z);
+            cen2[i / 2][4 * v + 3] = f2_pack(x.w, y.w);
+        }
+        // exact: a power-of-two scale
+        cn2[i / 2] = f2_pack(0.25f * __ldg(ix.pq_hi + e), 0.25f * __ldg(ix.pq_hi + e1));
+    }
 
     if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);
     for (;;) {
         __syncthreads();
         const int q = qslot[1];
         if (q >= a.nq) break;
-        __syncthreads();
-        if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
         // this query's probe count and result count (uneven batches)
         const int wq = query_w(a, q);
+        // its probe lists and their lengths, loaded by all threads at once (one memory round trip
+        // instead of two dependent ones per 32 probes); the prefix sums follow, in one warp
+        for (int j = tid; j < wq; j += NT) {
+            const int l = __ldg(a.probes + (int64_t)q * w + j);
+            plist[j] = l;
+            prefix[j] = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
+        }
+        if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
+        __syncthreads();
+        if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
         const int kq0 = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : query_k(a, q);
         // the precision form keeps alpha * k approximate candidates for the exact re-score
         const int kq = MIXED ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
-        if (!src_res && tid < D) xq[tid] = __ldg(a.queries + (int64_t)q * D + tid);
-        // probe lists and their prefix sums, one warp
+        // prefix sums of the probe lengths (each lane reads, then overwrites, its own slot)
         if (tid < 32) {
             uint32_t carry = 0;
             for (int j0 = 0; j0 < wq; j0 += 32) {
                 const int j = j0 + lane;
-                int l = -1;
-                uint32_t len = 0;
-                if (j < wq) {
-                    l = __ldg(a.probes + (int64_t)q * w + j);
-                    len = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
-                    plist[j] = l;
-                }
+                const uint32_t len = j < wq ? prefix[j] : 0u;
                 uint32_t incl = len;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -194,57 +236,26 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             if (lane == 0) prefix[wq] = carry;
         }
         topk_init(s, kq);
-        // precision form: this thread's per-query table term q3[i] = -2 <x_s, c_i> (its E entries)
-        float q3[MIXED ? E : 1];
-        if constexpr (MIXED) {
-            const float* xs = xq + my_s * DS;
+        // copy probe jj's first chunk of code groups into its stage (one commit group per probe,
+        // empty past the last probe, so that the group count stays in step with the probes)
+        auto stage_probe = [&](int jj) {
+            if constexpr (!MIXED) return;
+            const int ll = jj < wq ? plist[jj] : -1;
+            if (ll >= 0) {
+                const int ngp = (__ldg(ix.list_len + ll) + G - 1) / G;
+                const uint8_t* cp = ix.codes + __ldg(ix.list_beg + ll) * (int64_t)M;
+                uint4* dst = stage + (jj % SP_NS) * (US * NT);
 #pragma unroll
-            for (int i = 0; i < E; i++) {
-                const float4* c4 = reinterpret_cast<const float4*>(ix.pq + (int64_t)(my_s * KS + my_c0 + i) * DS);
-                float dt = 0.0f;
-#pragma unroll
-                for (int v = 0; v < DS / 4; v++) {
-                    const float4 c = __ldg(c4 + v);
-                    dt = __fmaf_rn(xs[4 * v], c.x, dt);
-                    dt = __fmaf_rn(xs[4 * v + 1], c.y, dt);
-                    dt = __fmaf_rn(xs[4 * v + 2], c.z, dt);
-                    dt = __fmaf_rn(xs[4 * v + 3], c.w, dt);
-                }
-                q3[i] = -2.0f * dt;
-            }
-        }
-
-        // precision form: the next probe's table terms and first code chunk load during this probe
-        // (its table build is a few adds, too short to hide an HBM round trip)
-        uint4 pre[MIXED ? U : 1];
-        float t2n[MIXED ? E : 1];
-        auto load_probe = [&](int jj) {
-            if constexpr (MIXED) {
-                const int ll = jj < wq ? plist[jj] : -1;
-                const int ngp = ll >= 0 ? (__ldg(ix.list_len + ll) + G - 1) / G : 0;
-                const uint8_t* cp = ix.codes + (ll >= 0 ? __ldg(ix.list_beg + ll) : 0) * (int64_t)M;
-#pragma unroll
-                for (int u = 0; u < U; u++) {
+                for (int u = 0; u < US; u++) {
                     const int g = u * NT + tid;
-                    pre[u] = g < ngp ? load_group(cp + (int64_t)g * 16) : make_uint4(0, 0, 0, 0);
-                }
-                const float* t2 = a.term2 + ((int64_t)(ll >= 0 ? ll : 0) * M + my_s) * KS + my_c0;
-                if constexpr (E % 4 == 0) {
-#pragma unroll
-                    for (int i = 0; i < E; i += 4) {
-                        const float4 v = ll >= 0 ? __ldg(reinterpret_cast<const float4*>(t2 + i)) : make_float4(0, 0, 0, 0);
-                        t2n[i] = v.x;
-                        t2n[i + 1] = v.y;
-                        t2n[i + 2] = v.z;
-                        t2n[i + 3] = v.w;
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < E; i++) t2n[i] = ll >= 0 ? __ldg(t2 + i) : 0.0f;
+                    if (g < ngp) cp_async16(dst + g, cp + (int64_t)g * 16);
                 }
             }
+            cp_async_commit();
         };
-        load_probe(0);
+#pragma unroll
+        for (int jj = 0; jj < SP_AHEAD; jj++) stage_probe(jj);
+
 
         for (int j = 0; j < wq; j++) {
             const int jr = j % SP_RCH;
@@ -265,20 +276,13 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                     for (int e = tid; e < nr * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
                 __syncthreads();
             }
-            uint4 cur[U];
-            float t2c[MIXED ? E : 1];
-            if constexpr (MIXED) {
-#pragma unroll
-                for (int u = 0; u < U; u++) cur[u] = pre[u];
-#pragma unroll
-                for (int i = 0; i < E; i++) t2c[i] = t2n[i];
-                load_probe(j + 1);
-            }
+            stage_probe(j + SP_AHEAD);
             const int l = plist[j];
             if (l < 0) continue;
             const int len = __ldg(ix.list_len + l);
             const int ng = (len + G - 1) / G;  // 16-byte groups of code rows
             const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
+            uint4 cur[U];
             if constexpr (!MIXED) {
                 // first chunk of codes in flight during the table build
 #pragma unroll
@@ -290,22 +294,40 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             float* table = tables + (j & 1) * (M * KS);
             __half* table16 = reinterpret_cast<__half*>(tables) + (j & 1) * (M * KS);
             if constexpr (MIXED) {
-                // approximate entry ||r_s - c||^2 = term2[l][s][c] + q3 + ||r_s||^2, where
-                // term2 = ||c||^2 + 2 <y_{l,s}, c> is precomputed per list: 2 adds per entry
-                const float f = rn[jr * M + my_s];
-                unsigned short h[E];
+                // approximate entry, scaled: ||r_s - c||^2 / 4 = ||r_s||^2 / 4 + ||c||^2 / 4 - <r_s, c> / 2,
+                // the dot product by packed fused multiply-adds over the register codebook (two
+                // entries per instruction), converted to FP16 in pairs with saturation
+                f2_t rs2[DS];
+                const float4* r4 = reinterpret_cast<const float4*>(rr + jr * D + my_s * DS);
 #pragma unroll
-                for (int i = 0; i < E; i++) h[i] = f16_sat((t2c[i] + q3[i] + f) * SP_T16_SCALE);
-                __half* dst = table16 + my_s * KS + my_c0;
+                for (int v4 = 0; v4 < DS / 4; v4++) {
+                    const float4 x = r4[v4];
+                    rs2[4 * v4] = f2_pack(x.x, x.x);
+                    rs2[4 * v4 + 1] = f2_pack(x.y, x.y);
+                    rs2[4 * v4 + 2] = f2_pack(x.z, x.z);
+                    rs2[4 * v4 + 3] = f2_pack(x.w, x.w);
+                }
+                const float f4 = SP_T16_SCALE * rn[jr * M + my_s];
+                const f2_t f42 = f2_pack(f4, f4), mh2 = f2_pack(-2.0f * SP_T16_SCALE, -2.0f * SP_T16_SCALE);
+                uint32_t hw[EM];
+#pragma unroll
+                for (int i = 0; i < EM; i++) {
+                    f2_t dt = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                    for (int t = 0; t < DS; t++) dt = f2_fma(rs2[t], cen2[i][t], dt);
+                    float e0, e1;
+                    f2_unpack(f2_fma(mh2, dt, f2_add(f42, cn2[i])), e0, e1);
+                    hw[i] = f16x2_sat(e0, e1);
+                }
+                uint32_t* dst = reinterpret_cast<uint32_t*>(table16 + my_s * KS + my_c0);
                 if constexpr (E == 8) {
-                    *reinterpret_cast<uint4*>(dst) =
-                        make_uint4(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16,
-                                   h[4] | (uint32_t)h[5] << 16, h[6] | (uint32_t)h[7] << 16);
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
                 } else if constexpr (E == 4) {
-                    *reinterpret_cast<uint2*>(dst) = make_uint2(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16);
+                    *reinterpret_cast<uint2*>(dst) = make_uint2(hw[0], hw[1]);
+                } else if constexpr (E == 2) {
+                    dst[0] = hw[0];
                 } else {
-#pragma unroll
-                    for (int i = 0; i < E; i++) reinterpret_cast<unsigned short*>(dst)[i] = h[i];
+                    *reinterpret_cast<unsigned short*>(dst) = (unsigned short)(hw[0] & 0xffffu);
                 }
             } else
             // table row segment from the register codebook
@@ -391,6 +413,18 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             if (flush_now) topk_flush(s, nb);
             // ADC scan of the list, software-pipelined one chunk ahead; the
             // filter compares floats first; warps past the end skip the chunk
+            // this probe's first chunk, from its stage (the thread's own copies: probes up to j
+            // have landed once at most SP_AHEAD groups remain in flight); groups past the staged
+            // 1024 (1024-thread blocks) come from global memory
+            if constexpr (MIXED) {
+                cp_async_wait<SP_AHEAD>();
+                const uint4* src = stage + (j % SP_NS) * (US * NT);
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int g = u * NT + tid;
+                    cur[u] = g >= ng ? make_uint4(0, 0, 0, 0) : (u < US ? src[g] : load_group(codes + (int64_t)g * 16));
+                }
+            }
             const uint32_t pos0 = prefix[j];
             const bool fits = len <= SP_BCAP - (flush_now ? 0 : nb);
             u64 tk = *s.thresh;
@@ -738,9 +772,10 @@ template <int M, bool DIRECT, int NT, bool MIXED = false>
 static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid) {
     const int kcap = scan_persistent_stride(a);
     if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
-    if (MIXED && (!a.term2 || !a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
+    if (MIXED && (!a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
     if ((a.flags & SCAN_REFINE) && (!a.cand_list || !ix.codes2 || !ix.pq2)) return cudaErrorInvalidValue;
-    ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH);
+    ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH, MIXED ? 2 : 4,
+                                  MIXED ? (size_t)SP_NS * std::min((M == 4 ? 1 : 2) * NT, 1024) * 16 : 0);
     auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT, MIXED>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
