@@ -49,6 +49,10 @@ struct ScanArgs {
     int32_t* out_ids = nullptr;
     float* out_dis = nullptr;
     int* queue = nullptr;              // work counter of the persistent kernel (zeroed per launch)
+    // -0.0f, passed at run time: the exact tables form each product as fma(r, c, -0), which rounds
+    // once like the reference's multiply; a -0 the compiler cannot see keeps it from treating the
+    // FMA as a multiply and fusing it into the following add
+    float neg_zero = -0.0f;
     // hand-off from the persistent scan to its finalize kernel: per query the
     // unsorted best keys and their base ids (cand_stride slots) and a count
     unsigned long long* cand_key = nullptr;

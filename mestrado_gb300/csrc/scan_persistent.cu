@@ -345,19 +345,21 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                 const float f = DIRECT ? 0.0f : rn[jr * M + my_s];
                 float out[E];
                 if constexpr (E % 2 == 0 && !DIRECT) {
-                    // The dot products stay scalar: ptxas contracts a packed multiply and add into a
-                    // fused multiply-add, which rounds differently from the reference's separate
-                    // operations. The multiply-free TwoSum of the norm sum and the final -2 dot + c
-                    // (-2 dot is exact, so fusing it changes nothing) run on packed pairs.
-                    const f2_t f2 = f2_pack(f, f), m2 = f2_pack(-2.0f, -2.0f);
+                    // Two entries per instruction. The dot products' products are fma(r, c, -0) with
+                    // a -0 known only at run time: ptxas contracts a packed multiply feeding a packed
+                    // add into a fused multiply-add (measured), which rounds differently from the
+                    // reference's separate operations, but it cannot merge two FMAs. The TwoSum of the
+                    // norm sum and the final -2 dot + c (-2 dot is exact, so fusing it changes
+                    // nothing) need no such guard.
+                    const f2_t f2 = f2_pack(f, f), m2 = f2_pack(-2.0f, -2.0f), nz2 = f2_pack(a.neg_zero, a.neg_zero);
 #pragma unroll
                     for (int i = 0; i < E; i += 2) {
-                        float d0 = 0.0f, d1 = 0.0f;
+                        f2_t d2 = f2_pack(0.0f, 0.0f);
 #pragma unroll
-                        for (int t = 0; t < DS; t++) {
-                            d0 = __fadd_rn(d0, __fmul_rn(rs[t], cen[i][t]));
-                            d1 = __fadd_rn(d1, __fmul_rn(rs[t], cen[i + 1][t]));
-                        }
+                        for (int t = 0; t < DS; t++)
+                            d2 = f2_add(d2, f2_fma(f2_pack(rs[t], rs[t]), f2_pack(cen[i][t], cen[i + 1][t]), nz2));
+                        float d0, d1;
+                        f2_unpack(d2, d0, d1);
                         const f2_t hi2 = f2_pack(nhi[i], nhi[i + 1]);
                         const f2_t S2 = f2_add(hi2, f2);
                         const f2_t bb = f2_sub(S2, hi2);
