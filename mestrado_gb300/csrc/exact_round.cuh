@@ -76,6 +76,13 @@ GB_HD float add_norms_rn(const double* Dp, float hi, float lo, float f) {
 }
 
 #if defined(__CUDACC__)
+// split_norm on the device
+__device__ __forceinline__ void split_norm_dev(double D, float* hi, float* lo) {
+    const float h = __double2float_rn(D);
+    *hi = h;
+    *lo = __double2float_rn(__dsub_rn(D, (double)h));
+}
+
 // the rounding decision of add_norms_rn, given S = RN32(hi + f) and t ~ (D + f) - S
 __device__ __forceinline__ float add_norms_finish(const double* Dp, float S, float t, float f) {
     const uint32_t sb = __float_as_uint(S);

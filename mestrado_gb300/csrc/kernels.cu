@@ -12,6 +12,8 @@
 // broken by (distance, payload) keys (block_topk.cuh).
 #include <algorithm>
 
+#include "exact_round.cuh"
+#include "f32x2.cuh"
 #include "scan_common.cuh"
 
 namespace gbivf {
@@ -48,73 +50,123 @@ cudaError_t launch_norm_f(const float* x, int64_t n, int d, float* out, cudaStre
 }
 
 // ---------------------------------------------------------------------------
-// coarse distances: 64 x 64 output tile per CTA, 4 x 4 per thread, K chunks
-// of 32 staged in shared memory. Every output is one sequential dot product
-// over l = 0..d-1 (the netlib sgemm order), then the expansion epilogue.
+// coarse distances: 128 x 128 output tile per CTA, 8 x 8 per thread (rows
+// 4ty..4ty+3 and 64+4ty.., columns likewise with tx), K chunks of 16 staged in
+// shared memory (the next chunk is loaded into registers while the current one
+// is used). Every output is one sequential dot product over l = 0..d-1 (the
+// netlib sgemm order), two outputs per instruction: each product is
+// fma(q, c, -0) with a -0 the compiler cannot see (so it rounds once, like the
+// reference's multiply, and is not fused into the add), each sum a packed add.
+// Epilogue: the reference's constant term (float)(double ||q||^2 + float
+// ||c||^2) by the exact FP32 form of that sum (exact_round.cuh; GB300's FP64
+// rate is a small fraction of FP32), then -2 dot + c.
 // ---------------------------------------------------------------------------
 
-constexpr int CD_TILE = 64, CD_K = 32;
+constexpr int CD_TILE = 128, CD_K = 16;
 
 __global__ void __launch_bounds__(256) coarse_dist_kernel(
     const float* __restrict__ X, int nq, const float* __restrict__ Cc, int C, int d,
     const double* __restrict__ qnorm, const float* __restrict__ cnorm, float* __restrict__ out,
-    CoarseFilter flt) {
-    __shared__ float Xs[CD_K][CD_TILE + 1];
-    __shared__ float Cs[CD_K][CD_TILE + 1];
+    CoarseFilter flt, float neg_zero) {
+    __shared__ __align__(16) float Xs[CD_K][CD_TILE];
+    __shared__ __align__(16) float Cs[CD_K][CD_TILE];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int q0 = blockIdx.y * CD_TILE, c0 = blockIdx.x * CD_TILE;
-    float acc[4][4];
+    // 16-byte loads where every row starts on a 16-byte boundary
+    const bool vec = (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(Cc)) & 15) == 0;
+    const f2_t nz2 = f2_pack(neg_zero, neg_zero);
+    f2_t acc[8][4];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+        for (int j = 0; j < 4; j++) acc[i][j] = f2_pack(0.0f, 0.0f);
 
+    // staging: element (row r, 4 columns from l0 + 4v) for e = tid + 256 h, r = e % 128, v = e / 128
+    float4 px[2], pc[2];
+    auto fetch = [&](int l0) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int e = tid + 256 * h, r = e & 127, l = l0 + 4 * (e >> 7);
+            const int qr = q0 + r, cr = c0 + r;
+            float4 x = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = x;
+            if (vec) {
+                if (qr < nq && l < d) x = __ldg(reinterpret_cast<const float4*>(X + (int64_t)qr * d + l));
+                if (cr < C && l < d) c = __ldg(reinterpret_cast<const float4*>(Cc + (int64_t)cr * d + l));
+            } else {
+                float xv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (qr < nq && l + k < d) xv[k] = X[(int64_t)qr * d + l + k];
+                    if (cr < C && l + k < d) cv[k] = Cc[(int64_t)cr * d + l + k];
+                }
+                x = make_float4(xv[0], xv[1], xv[2], xv[3]);
+                c = make_float4(cv[0], cv[1], cv[2], cv[3]);
+            }
+            px[h] = x;
+            pc[h] = c;
+        }
+    };
+    fetch(0);
     for (int l0 = 0; l0 < d; l0 += CD_K) {
-        for (int e = tid; e < CD_TILE * CD_K; e += 256) {
-            int row = e / CD_K, col = e % CD_K;
-            int l = l0 + col;
-            int qr = q0 + row, cr = c0 + row;
-            Xs[col][row] = (qr < nq && l < d) ? X[(int64_t)qr * d + l] : 0.0f;
-            Cs[col][row] = (cr < C && l < d) ? Cc[(int64_t)cr * d + l] : 0.0f;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int e = tid + 256 * h, r = e & 127, k = 4 * (e >> 7);
+            Xs[k][r] = px[h].x;
+            Xs[k + 1][r] = px[h].y;
+            Xs[k + 2][r] = px[h].z;
+            Xs[k + 3][r] = px[h].w;
+            Cs[k][r] = pc[h].x;
+            Cs[k + 1][r] = pc[h].y;
+            Cs[k + 2][r] = pc[h].z;
+            Cs[k + 3][r] = pc[h].w;
         }
         __syncthreads();
+        if (l0 + CD_K < d) fetch(l0 + CD_K);
         const int lmax = min(CD_K, d - l0);
         for (int l = 0; l < lmax; l++) {
-            float a[4], b[4];
+            const float4 a0 = reinterpret_cast<const float4*>(Xs[l])[ty];
+            const float4 a1 = reinterpret_cast<const float4*>(Xs[l])[16 + ty];
+            const float4 b0 = reinterpret_cast<const float4*>(Cs[l])[tx];
+            const float4 b1 = reinterpret_cast<const float4*>(Cs[l])[16 + tx];
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const f2_t b[4] = {f2_pack(b0.x, b0.y), f2_pack(b0.z, b0.w), f2_pack(b1.x, b1.y), f2_pack(b1.z, b1.w)};
 #pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = Xs[l][ty + 16 * i];
+            for (int i = 0; i < 8; i++) {
+                const f2_t aa = f2_pack(a[i], a[i]);
 #pragma unroll
-            for (int j = 0; j < 4; j++) b[j] = Cs[l][tx + 16 * j];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] = __fadd_rn(acc[i][j], __fmul_rn(b[j], a[i]));
+                for (int j = 0; j < 4; j++) acc[i][j] = f2_add(acc[i][j], f2_fma(aa, b[j], nz2));
+            }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        int q = q0 + ty + 16 * i;
+    for (int i = 0; i < 8; i++) {
+        const int q = q0 + (i < 4 ? 4 * ty + i : 64 + 4 * ty + i - 4);
         if (q >= nq) continue;
-        double qn = qnorm[q];
-#pragma unroll
-        if (flt.thr) {
-            // filtered: append the centroids within the query's bound
-            const float T = flt.thr[q];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                int c = c0 + tx + 16 * j;
-                if (c < C && expansion_from(qn, cnorm[c], acc[i][j]) <= T) {
-                    const int slot = atomicAdd(&flt.ncand[q], 1);
-                    if (slot < flt.cap) flt.cand[(int64_t)q * flt.cap + slot] = c;
-                }
-            }
-            continue;
-        }
+        const double qn = qnorm[q];
+        float qhi, qlo;
+        split_norm_dev(qn, &qhi, &qlo);
+        const float T = flt.thr ? flt.thr[q] : 0.0f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            int c = c0 + tx + 16 * j;
-            if (c < C) out[(int64_t)q * C + c] = expansion_from(qn, cnorm[c], acc[i][j]);
+            float dot[2];
+            f2_unpack(acc[i][j], dot[0], dot[1]);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = c0 + (j < 2 ? 4 * tx + 2 * j + h : 64 + 4 * tx + 2 * (j - 2) + h);
+                if (c >= C) continue;
+                const float cst = add_norms_rn(qnorm + q, qhi, qlo, cnorm[c]);
+                const float dist = __fadd_rn(__fmul_rn(-2.0f, dot[h]), cst);
+                if (flt.thr) {
+                    // filtered: append the centroids within the query's bound
+                    if (dist <= T) {
+                        const int slot = atomicAdd(&flt.ncand[q], 1);
+                        if (slot < flt.cap) flt.cand[(int64_t)q * flt.cap + slot] = c;
+                    }
+                } else {
+                    out[(int64_t)q * C + c] = dist;
+                }
+            }
         }
     }
 }
@@ -123,7 +175,8 @@ cudaError_t launch_coarse_dist(const DevIndex& ix, const float* q, const double*
                                float* out, cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
     dim3 grid((ix.C + CD_TILE - 1) / CD_TILE, (nq + CD_TILE - 1) / CD_TILE);
-    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, out, CoarseFilter{});
+    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, out, CoarseFilter{},
+                                             -0.0f);
     return cudaGetLastError();
 }
 
@@ -132,7 +185,7 @@ cudaError_t launch_coarse_dist_filter(const DevIndex& ix, const float* q, const 
     if (nq <= 0) return cudaSuccess;
     if (!f.thr || !f.ncand || !f.cand || f.cap <= 0) return cudaErrorInvalidValue;
     dim3 grid((ix.C + CD_TILE - 1) / CD_TILE, (nq + CD_TILE - 1) / CD_TILE);
-    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, nullptr, f);
+    coarse_dist_kernel<<<grid, 256, 0, st>>>(q, nq, ix.coa, ix.C, ix.d, qnorm, ix.coa_norm, nullptr, f, -0.0f);
     return cudaGetLastError();
 }
 
