@@ -80,6 +80,32 @@ __device__ __forceinline__ void topk_push(TopKSmem& s, u64 key, bool pass) {
     if (pass) s.buf[base + __popc(mask & ((1u << lane) - 1u))] = key;
 }
 
+// Warp-collective append of R keys per lane (row r of every lane, then row r + 1, ...) with one
+// shared atomic for all of them; the caller has checked that some lane passes.
+template <int R>
+__device__ __forceinline__ void topk_push_rows(TopKSmem& s, const u64 (&key)[R], const bool (&pass)[R]) {
+    const int lane = threadIdx.x & 31;
+    unsigned msk[R], all = 0;
+    int total = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        msk[r] = __ballot_sync(0xffffffffu, pass[r]);
+        all |= msk[r];
+        total += __popc(msk[r]);
+    }
+    if (all == 0) return;
+    const int leader = __ffs(all) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(s.nbuf, total);
+    base = __shfl_sync(0xffffffffu, base, leader);
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        if (pass[r]) s.buf[base + __popc(msk[r] & lt)] = key[r];
+        base += __popc(msk[r]);
+    }
+}
+
 __device__ inline void bitonic_sort_smem(u64* a, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int size = 2; size <= n; size <<= 1) {

@@ -236,6 +236,9 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             if (lane == 0) prefix[wq] = carry;
         }
         topk_init(s, kq);
+        // buffered keys that trigger a flush at a list boundary: a flush selects among the best kq
+        // and the buffer, so with a large kq (the precision form's 4k) a larger buffer amortises it
+        const int soft = max(SP_SOFT, min(kq, SP_BCAP / 2));
         // copy probe jj's first chunk of code groups into its stage (one commit group per probe,
         // empty past the last probe, so that the group count stays in step with the probes)
         auto stage_probe = [&](int jj) {
@@ -410,7 +413,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             // count is read between it and the next one, before new appends
             __syncthreads();
             const int nb = *s.nbuf;
-            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kq && nb >= kq) || nb >= SP_SOFT;
+            const bool flush_now = (nb + len > SP_BCAP) || (*s.nbest < kq && nb >= kq) || nb >= soft;
             __syncthreads();
             if (flush_now) topk_flush(s, nb);
             // ADC scan of the list, software-pipelined one chunk ahead; the
@@ -456,9 +459,10 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
                             any |= pass[r];
                         }
                         if (__any_sync(0xffffffffu, any)) {
+                            u64 key[G];
 #pragma unroll
-                            for (int r = 0; r < G; r++)
-                                topk_push(s, make_key(dist[r], pos0 + (uint32_t)(i0 + r)), pass[r]);
+                            for (int r = 0; r < G; r++) key[r] = make_key(dist[r], pos0 + (uint32_t)(i0 + r));
+                            topk_push_rows<G>(s, key, pass);
                         }
                     }
                 }
