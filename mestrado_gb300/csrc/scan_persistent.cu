@@ -490,24 +490,62 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             topk_flush(s, nb);
         }
         const int nbest = *s.nbest;
-        for (int c = tid; c < a.cand_stride; c += NT) {
-            const int64_t o = (int64_t)q * a.cand_stride + c;
-            if (c < nbest) {
-                a.cand_key[o] = best[c];
-                if (rows_out) {
-                    // the code row and its list, for the exact re-score or the refinement re-rank
-                    const uint32_t pos = key_payload(best[c]);
-                    const int jj = probe_of(prefix, wq, pos);
-                    const int ll = plist[jj];
-                    a.cand_id[o] = (int32_t)(ix.list_beg[ll] + (int64_t)(pos - prefix[jj]));
-                    a.cand_list[o] = ll;
-                } else {
-                    a.cand_id[o] = pos_to_id(ix, prefix, plist, wq, key_payload(best[c]));
+        if (rows_out) {
+            // The code row and its list of each candidate, for the exact re-score or the refinement
+            // re-rank, grouped by probe (a counting sort on probe & 255): neighbouring threads of the
+            // finalize kernel then read the same list centroid and nearby code rows. The finalize
+            // orders candidates by (distance, position) keys, so the slot order is free.
+            int* cnt = s.hist(0);
+            for (int i = tid; i < 256; i += NT) cnt[i] = 0;
+            __syncthreads();
+            for (int c = tid; c < nbest; c += NT) atomicAdd(&cnt[probe_of(prefix, wq, key_payload(best[c])) & 255], 1);
+            __syncthreads();
+            if (tid < 32) {  // exclusive prefix over the 256 bins, 8 per lane
+                int v[8], sum = 0;
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    v[b] = cnt[8 * lane + b];
+                    sum += v[b];
                 }
-            } else {
+                int incl = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                int run = incl - sum;
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    cnt[8 * lane + b] = run;
+                    run += v[b];
+                }
+            }
+            __syncthreads();
+            for (int c = tid; c < nbest; c += NT) {
+                const uint32_t pos = key_payload(best[c]);
+                const int jj = probe_of(prefix, wq, pos);
+                const int ll = plist[jj];
+                const int64_t o = (int64_t)q * a.cand_stride + atomicAdd(&cnt[jj & 255], 1);
+                a.cand_key[o] = best[c];
+                a.cand_id[o] = (int32_t)(ix.list_beg[ll] + (int64_t)(pos - prefix[jj]));
+                a.cand_list[o] = ll;
+            }
+            for (int c = nbest + tid; c < a.cand_stride; c += NT) {
+                const int64_t o = (int64_t)q * a.cand_stride + c;
                 a.cand_key[o] = KEY_MAX;
                 a.cand_id[o] = -1;
-                if (rows_out) a.cand_list[o] = 0;
+                a.cand_list[o] = 0;
+            }
+        } else {
+            for (int c = tid; c < a.cand_stride; c += NT) {
+                const int64_t o = (int64_t)q * a.cand_stride + c;
+                if (c < nbest) {
+                    a.cand_key[o] = best[c];
+                    a.cand_id[o] = pos_to_id(ix, prefix, plist, wq, key_payload(best[c]));
+                } else {
+                    a.cand_key[o] = KEY_MAX;
+                    a.cand_id[o] = -1;
+                }
             }
         }
         if (tid == 0) a.cand_cnt[q] = nbest;
