@@ -46,8 +46,8 @@ extern "C" {
                                    select from it, instead of the default sample-bound candidate filter;
                                    the results are the same either way */
 #define GBIVF_MIXED_SCAN 0x10u  /* precision form of the scan (d = 128, ks = 256, m in {4, 8, 16}): PQ tables
-                                   built approximately from per-list terms and held in FP16, summed in
-                                   FP32; the GBIVF_MIXED_SCAN_ALPHA * k best (at most 4096) are re-scored
+                                   built approximately (packed fused multiply-adds) and held in FP16,
+                                   summed in FP32; the GBIVF_MIXED_SCAN_ALPHA * k best (at most 4096) are re-scored
                                    in the reference's FP32 arithmetic, so every returned distance is the
                                    plain form's and the ids match it unless a true neighbour fell outside
                                    the approximate selection */

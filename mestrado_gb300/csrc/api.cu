@@ -127,7 +127,7 @@ struct gbivf_index {
     DBuf coa_tiles, coa_len, coa_colG, coa_colK, w_qtiles, w_flags;
     // filtered coarse stage (large C): per-query bounds, counters, candidate slots, GEMM survivors
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
-    // precision form of the scan: per-list table terms (C x m x 256), hand-off lists
+    // hand-off lists of the precision form and the refinement re-rank
     DBuf w_clist;
     // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

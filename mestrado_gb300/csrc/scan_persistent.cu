@@ -4,14 +4,16 @@
 //
 // One CTA of 512 threads per SM pulls queries from a device work counter.
 // The whole PQ codebook (m x 256 x ds = 32768 floats) lives in registers:
-// thread t owns table entries e = t + 512 i (i < m/2), i.e. 64 centroid
-// floats, loaded once per launch. For each probed list of a query the block
+// thread t owns the E = m*256/512 consecutive table entries of one
+// sub-quantizer, i.e. 64 centroid floats, loaded once per launch. For each
+// probed list of a query the block
 //   1. forms the residual r = x - c_list in shared memory (bsxfunMINUS),
 //   2. computes the m sub-norms of r,
-//   3. builds the m x 256 table from registers -- per entry a sequential
-//      float dot product and the reference's norm sum (exact_round.cuh),
-//      no memory traffic for the centroids,
-//   4. streams the list's codes (8/16-byte vector loads) through the ADC sum
+//   3. builds the m x 256 table from registers, two entries per packed
+//      instruction -- exact form: per entry a sequential float dot product and
+//      the reference's norm sum (exact_round.cuh); precision form: FP16
+//      entries by fused multiply-adds -- with no memory traffic for centroids,
+//   4. streams the list's codes (16-byte groups of rows) through the ADC sum
 //      and the threshold filter of the block top-k.
 // The top-k buffer is sized so that a whole list fits: the capacity check is
 // made once per list at a barrier that exists anyway, and the scan loop runs
