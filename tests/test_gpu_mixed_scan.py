@@ -93,3 +93,39 @@ def test_mixed_scan_rejects_direct_tables():
         gi.search(g.queries, 10, 4, direct=True, mixed_scan=True)
     assert e.value.code == 4
     gi.close()
+
+
+@pytest.fixture(scope="module")
+def long_list_indexes():
+    """GPU-built indexes with few, long lists (~4,700 codes each on average), m = 4, 8 and 16, so
+    that probes span several code chunks and more code groups than the precision form stages."""
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
+    from mestrado_gb300.synth import Mixture
+
+    gm = GpuMixture(Mixture(d=128, ncomp=64, seed=21))
+    base = gm.generate(300000, stream_id=1)
+    train = gm.generate(40000, stream_id=2)
+    q = gm.generate(200, stream_id=3).cpu().numpy()
+    out = {m: build_index_gpu(base, train, coarsek=64, m=m, niter=4, seed=3) for m in (4, 8, 16)}
+    return out, q
+
+
+@pytest.mark.parametrize("threads", ["512", "1024"])
+@pytest.mark.parametrize("m", [4, 8, 16])
+def test_mixed_scan_long_lists_every_shape(long_list_indexes, m, threads, monkeypatch):
+    """Every sub-quantizer count and block size of the precision form (at 1024 threads and m = 4
+    each thread holds a single table entry; past 1024 code groups a probe's codes come from global
+    memory instead of the stage): distances bit-identical to the plain form's for every shared id."""
+    from mestrado_gb300.engine import GpuIndex
+
+    monkeypatch.setenv("GBIVF_SCAN_THREADS", threads)
+    ixs, q = long_list_indexes
+    gi = GpuIndex(ixs[m])
+    for k, w in ((10, 3), (100, 8)):
+        a = gi.search(q, k, w)
+        b = gi.search(q, k, w, mixed_scan=True)
+        same, ok = compare(a[0], a[1], b[0], b[1])
+        print(f"m={m} threads={threads} k={k} w={w}: identical rows {same:.4f}")
+        assert ok, "a returned distance differs from the plain form's"
+        assert same >= 0.99
+    gi.close()
