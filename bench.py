@@ -162,21 +162,44 @@ class ClockSampler:
         self.p = None
 
     def start(self):
+        """Start polling (every 50 ms) and return once the first sample has arrived, so that the
+        timed region that follows is covered from its start."""
+        import threading
+
+        self.lines = []
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
+            return
+        first = threading.Event()
+
+        def reader():
+            for line in self.p.stdout:
+                self.lines.append(line)
+                first.set()
+            first.set()
+
+        self.t = threading.Thread(target=reader, daemon=True)
+        self.t.start()
+        first.wait(timeout=10)
+        self.skip = len(self.lines)  # samples taken before the timed region
 
     def stop(self):
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
-        out, _ = self.p.communicate(timeout=10)
+        try:
+            self.p.wait(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=10)
+        lines = self.lines[self.skip:] or self.lines[-1:]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in out.strip().splitlines():
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 7:
                 continue
@@ -732,7 +755,7 @@ def sp_ptr(s):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbivf", choices=["gbivf", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS) + sorted(LARGE))
