@@ -239,13 +239,40 @@ def profiled_traffic(config_name):
 # CPU baseline (the oracle restatement of the reference, all host threads)
 # ---------------------------------------------------------------------------
 
-def cpu_search(ix, base, queries, c, nthreads):
+def cpu_search(ix, base, queries, c, nthreads, results=False):
     import oracle
 
     t = time.perf_counter()
-    oracle.ivfpq_search(ix, queries, k=c["k"], kl=c["kl"], w=c["w"], base=base, rerank=c["rerank"],
-                        nthreads=nthreads)
-    return time.perf_counter() - t
+    ids, dis = oracle.ivfpq_search(ix, queries, k=c["k"], kl=c["kl"], w=c["w"], base=base, rerank=c["rerank"],
+                                   nthreads=nthreads)
+    t = time.perf_counter() - t
+    return (t, ids, dis) if results else t
+
+
+def parity_report(g_ids, g_dis, o_ids, o_dis):
+    """The engine's results against the oracle's on the same queries: identical rows, and every id
+    both return carrying the same distance bits (the oracle keeps the reference's heap tie order,
+    the engine orders ties by (distance, id), so rows can differ only at ties)."""
+    n = len(o_ids)
+    same = float(np.mean([np.array_equal(g_ids[i], o_ids[i]) for i in range(n)]))
+
+    def up_to_ties(i):
+        # the same distance bits in the same positions, and the same ids at every distance but the
+        # last (a tie across the k-th position can keep different members)
+        gd, od = g_dis[i].view(np.uint32), o_dis[i].view(np.uint32)
+        if not np.array_equal(gd, od):
+            return False
+        last = gd[-1]
+        return set(g_ids[i][gd != last].tolist()) == set(o_ids[i][od != last].tolist())
+
+    ties_ok = float(np.mean([up_to_ties(i) for i in range(n)]))
+    mism = 0
+    for i in range(n):
+        o = dict(zip(o_ids[i].tolist(), o_dis[i].view(np.uint32).tolist()))
+        mism += sum(int(x in o and o[x] != y) for x, y in zip(g_ids[i].tolist(), g_dis[i].view(np.uint32).tolist()))
+    return {"queries": n, "identical_rows": same, "identical_rows_up_to_ties": ties_ok,
+            "distance_mismatches_on_shared_ids": mism,
+            "ties": "oracle in the reference's heap tie order; engine ties ordered by (distance, id)"}
 
 
 def run_reference(args, c, rank, world):
@@ -297,7 +324,7 @@ def run_gpu(args, c, rank, world, local_rank):
         nthreads = os.cpu_count() or 1
         sample = min(nq, args.ref_sample)
         cpu_search(ix_data, base, queries[: max(1, sample // 10)], c, nthreads)
-        t = cpu_search(ix_data, base, queries[:sample], c, nthreads)
+        t, cpu_ids, cpu_dis = cpu_search(ix_data, base, queries[:sample], c, nthreads, results=True)
         cpu = {"value": sample / t, "unit": "queries/s", "cores": nthreads, "kind": "port",
                "sample": f"{sample} queries of this workload, OpenMP over queries ({t:.2f}s)"}
 
@@ -318,6 +345,7 @@ def run_gpu(args, c, rank, world, local_rank):
     coaidx, _ = gi.coarse_assign(queries, w)
     sizes = ix_data.list_sizes().astype(np.int64)
     scan_bytes = int(sizes[coaidx].sum()) * m
+    unique_bytes = int(sizes[np.unique(coaidx[coaidx >= 0])].sum()) * m  # each probed list once
 
     for i in range(args.warmup):
         with torch.cuda.stream(stream):
@@ -380,9 +408,11 @@ def run_gpu(args, c, rank, world, local_rank):
 
     # quality (outside every timed region)
     quality = {}
+    if cpu is not None:
+        quality["parity_vs_oracle"] = parity_report(h_ids[:len(cpu_ids)], h_dis[:len(cpu_ids)], cpu_ids, cpu_dis)
     if rank == 0 and not args.no_recall:
         gt = ground_truth(base, queries, k, key, dev)
-        quality = recall_report(h_ids, gt, k)
+        quality.update(recall_report(h_ids, gt, k))
 
     peak, peak_kind = measured_peak_hbm()
     # the scan kernel alone (CUDA events on the engine's stream around its launch)
@@ -402,7 +432,8 @@ def run_gpu(args, c, rank, world, local_rank):
                     "d2h_bytes_per_step": int(nq * k * 8)},
             "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "bytes_per_launch": scan_bytes, "traffic": traffic},
+                         "bytes_per_launch": scan_bytes, "bytes_unique_per_launch": unique_bytes,
+                         "traffic": traffic},
             "cpu_baseline": cpu,
             # norm_d, coarse_dist, coarse_select, ivf_scan_persistent, finalize per search
             "gpu_launches": 5 * args.steps,
@@ -492,6 +523,8 @@ def run_large(args, c, name, local_rank):
     # candidate bytes of the ADC scan: sum over queries of their probed lists' codes
     coa_idx, _ = gi.coarse_assign(queries.cpu().numpy(), max_w)
     scan_bytes = int(sum(sizes[coa_idx[i, :wq[i]]].sum() for i in range(nq))) * c["m"]
+    probed = np.unique(np.concatenate([coa_idx[i, :wq[i]] for i in range(nq)]))
+    unique_bytes = int(sizes[probed[probed >= 0]].astype(np.int64).sum()) * c["m"]
     sample = 0 if args.no_recall else min(nq, c["recall_q"])
     gt = exact_topk(base, queries[:sample], max_k, batch=16 if c["nbase"] > 20_000_000 else 64) if sample else None
     del base
@@ -570,7 +603,7 @@ def run_large(args, c, name, local_rank):
                    "index_build_s": t_build, "generate_s": t_gen, "l2": "flushed between steps (256 MB write)"},
         "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": scan_bytes,
-                     "traffic": None},
+                     "bytes_unique_per_launch": unique_bytes, "traffic": None},
         "cpu_baseline": None,
         "clocks": mx["clocks"],
     }

@@ -43,3 +43,29 @@ def test_adc_error_fp64_zero_for_rounded_exact_and_sees_perturbation():
     pad_ids = res_ids.copy()
     pad_ids[2] = -1
     assert bench.adc_error_fp64(ix, q, (pad_ids, res_dis), off, kq, 2)["pairs"] == 5
+
+
+def test_parity_report_counts_rows_and_distance_bits():
+    import bench
+
+    g = np.array([[1, 2, 3], [4, 5, 6]], np.int32)
+    gd = np.array([[1, 2, 3], [4, 5, 6]], np.float32)
+    o = np.array([[1, 2, 3], [4, 6, 5]], np.int32)  # a tie order difference in row 1
+    od = np.array([[1, 2, 3], [4, 6, 5]], np.float32)
+    r = bench.parity_report(g, gd, o, od)
+    assert r["identical_rows"] == 0.5 and r["distance_mismatches_on_shared_ids"] == 0
+    od[0, 1] = np.nextafter(np.float32(2), np.float32(3))  # one ulp off for id 2
+    assert bench.parity_report(g, gd, o, od)["distance_mismatches_on_shared_ids"] == 1
+
+
+def test_parity_report_up_to_ties():
+    import bench
+
+    g = np.array([[1, 2, 3, 4], [5, 6, 7, 8]], np.int32)
+    gd = np.array([[1, 2, 2, 3], [1, 2, 3, 3]], np.float32)
+    o = np.array([[1, 3, 2, 4], [5, 6, 7, 9]], np.int32)  # tie order inside; a different boundary member
+    od = gd.copy()
+    r = bench.parity_report(g, gd, o, od)
+    assert r["identical_rows"] == 0.0 and r["identical_rows_up_to_ties"] == 1.0
+    o2 = np.array([[1, 9, 2, 4], [5, 6, 7, 8]], np.int32)  # a different id below the boundary
+    assert bench.parity_report(g, gd, o2, od)["identical_rows_up_to_ties"] == 0.5
