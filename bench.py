@@ -303,6 +303,23 @@ def run_reference(args, c, rank, world):
 # GPU engine
 # ---------------------------------------------------------------------------
 
+def max_over_ranks(x, dist, device):
+    """The slowest rank's time: every rank takes part in the reduction (None: one process)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(nq_per_rank, steps, world, seconds):
+    """Queries per second of the whole job: every rank searches its own nq_per_rank queries per
+    step (weak scaling), timed by the slowest rank."""
+    return nq_per_rank * steps * world / seconds
+
+
 def run_gpu(args, c, rank, world, local_rank):
     import torch
 
@@ -319,7 +336,7 @@ def run_gpu(args, c, rank, world, local_rank):
     nq, k, kl, w, m = c["nq"], c["k"], c["kl"], c["w"], c["m"]
 
     # CPU baseline first (rank 0, N=1), before any GPU work in this process
-    cpu = None
+    cpu = cpu_1core = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         sample = min(nq, args.ref_sample)
@@ -327,6 +344,11 @@ def run_gpu(args, c, rank, world, local_rank):
         t, cpu_ids, cpu_dis = cpu_search(ix_data, base, queries[:sample], c, nthreads, results=True)
         cpu = {"value": sample / t, "unit": "queries/s", "cores": nthreads, "kind": "port",
                "sample": f"{sample} queries of this workload, OpenMP over queries ({t:.2f}s)"}
+        # the reference's own search is single-threaded (sequential/ivf_pq/ivf_search.cpp): one core too
+        s1 = max(1, sample // 10)
+        t1 = cpu_search(ix_data, base, queries[:s1], c, 1)
+        cpu_1core = {"value": s1 / t1, "unit": "queries/s", "cores": 1, "kind": "port",
+                     "sample": f"{s1} queries of this workload, one thread ({t1:.2f}s)"}
 
     gi = GpuIndex(ix_data, device=local_rank, base=base)
     stream = torch.cuda.Stream(device=dev)
@@ -380,12 +402,8 @@ def run_gpu(args, c, rank, world, local_rank):
         fin_ms.append(fm)
     barrier()
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = nq * args.steps * world / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(step_ms), dist, dev)
+    value = whole_job_rate(nq, args.steps, world, total_ms / 1000.0)
 
     # end to end through the host C ABI: pinned host queries in, ids/dis out
     h_q = torch.from_numpy(queries).pin_memory().numpy()
@@ -400,16 +418,14 @@ def run_gpu(args, c, rank, world, local_rank):
         t = time.perf_counter()
         gi.search(h_q, k, w, kl=kl, rerank=c["rerank"], out=(h_ids, h_dis))
         e2e_s += time.perf_counter() - t
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = nq * args.steps * world / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist, dev)
+    e2e = whole_job_rate(nq, args.steps, world, e2e_s)
 
     # quality (outside every timed region)
     quality = {}
     if cpu is not None:
         quality["parity_vs_oracle"] = parity_report(h_ids[:len(cpu_ids)], h_dis[:len(cpu_ids)], cpu_ids, cpu_dis)
+        quality["cpu_baseline_1core"] = cpu_1core
     if rank == 0 and not args.no_recall:
         gt = ground_truth(base, queries, k, key, dev)
         quality.update(recall_report(h_ids, gt, k))
