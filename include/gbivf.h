@@ -57,6 +57,13 @@ extern "C" {
                                      raw vectors (needs gbivf_index_set_refine; k <= kl <= 1024). FP32:
                                      sequential sums over the 8 blocks of 16 dimensions, then the 8
                                      partial sums in block order */
+#define GBIVF_MIXED_SCAN_AUTO 0x40u /* the engine picks the scan form: the precision form (as
+                                     GBIVF_MIXED_SCAN) where gbivf_index_autotune, called with this flag,
+                                     measured it faster on this index, else the exact form; on an index
+                                     not tuned so, the precision form when m = 16 (its table build is
+                                     cheap against the 4096-entry exact table). Falls back to the exact
+                                     form where the precision form does not apply. Not combined with
+                                     GBIVF_MIXED_SCAN */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -171,6 +178,9 @@ int gbivf_graph_destroy(gbivf_graph *g);
  * variant's scan time, -1 where it does not apply. When the environment
  * variable GBIVF_TUNE_CACHE names a file, choices are read from and appended
  * to it, keyed by index shape, list-size histogram, GPU and search shape. */
+/* The scan form GBIVF_MIXED_SCAN_AUTO resolves to on this index: *tuned = 1 once gbivf_index_autotune
+ * measured it (with that flag), *mixed = 1 for the precision form. No counterpart in the reference. */
+int gbivf_index_scan_form(const gbivf_index *ix, int *tuned, int *mixed);
 int gbivf_index_autotune(gbivf_index *ix, const float *d_queries, int nq, int k, int kl, int w,
                          unsigned flags, int *choice, float *times_ms);
 

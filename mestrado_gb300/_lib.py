@@ -17,6 +17,7 @@ GBIVF_MIXED_COARSE = 0x4
 GBIVF_COARSE_FULL = 0x8
 GBIVF_MIXED_SCAN = 0x10
 GBIVF_RERANK_REFINE = 0x20
+GBIVF_MIXED_SCAN_AUTO = 0x40
 GBIVF_PROFILE = 0x100
 
 _lib = None
@@ -31,7 +32,7 @@ EXPORTS = [
     "gbivf_graph_destroy", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
     "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats", "gbivf_coarse_assign_device",
     "gbivf_index_set_refine", "gbivf_index_set_refine_device", "gbivf_pq_error", "gbivf_index_create_device",
-    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_selftest_wait_timeout",
+    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_selftest_wait_timeout", "gbivf_index_scan_form",
 ]
 
 
@@ -68,6 +69,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_pq_search.argtypes = [vp, vp, i32, i32, vp, vp]
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     lib.gbivf_last_stages_ms.argtypes = [vp, vp, vp, vp]
+    lib.gbivf_index_scan_form.argtypes = [vp, vp, vp]
     lib.gbivf_selftest_wait_timeout.argtypes = [C.c_int, vp, vp, vp]
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
     lib.gbivf_coarse_assign_flags.argtypes = [vp, vp, i32, i32, u32, vp, vp, vp]

@@ -116,6 +116,8 @@ struct gbivf_index {
     int64_t last_fallbacks = 0;       // queries of it that took all C centroids exactly
     float clen_max = 0.0f, cn_max = 0.0f;  // maxima of the centroid lengths / squared norms (mixed form)
     bool use_persistent = true;       // register-codebook scan where the shape allows
+    bool auto_tuned = false;          // GBIVF_MIXED_SCAN_AUTO: measured by the autotuner ...
+    bool auto_mixed = false;          // ... and the precision form was the faster
     int scan_threads = 512;           // block size of the persistent scan (512 or 1024)
     std::vector<void*> owned;    // index allocations
     DBuf base, base_norm;
@@ -366,8 +368,10 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
     if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL |
-                  GBIVF_MIXED_SCAN | GBIVF_RERANK_REFINE))
+                  GBIVF_MIXED_SCAN | GBIVF_RERANK_REFINE | GBIVF_MIXED_SCAN_AUTO))
         return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_MIXED_SCAN_AUTO))
+        return fail(GBIVF_ERR_INVALID, "GBIVF_MIXED_SCAN_AUTO chooses the scan form: not with GBIVF_MIXED_SCAN");
     if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_TABLE_DIRECT))
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN uses the expansion tables (not GBIVF_TABLE_DIRECT)");
     if (flags & GBIVF_RERANK_REFINE) {
@@ -590,10 +594,26 @@ int check_device_flags(gbivf_index* ix) {
 
 // queries already on the device; everything enqueued on st
 // (uneven batches: d_w / d_k / d_off per query, w and k their maxima; NULL = uniform)
+// whether the precision-form scan serves this index and search shape (scan_persistent_supported)
+bool mixed_scan_applies(const DevIndex& dx, int k, int kl, unsigned flags) {
+    const int kk = (flags & (GBIVF_RERANK | GBIVF_RERANK_REFINE)) ? kl : k;
+    return dx.d == 128 && dx.ks == 256 && (dx.m == 4 || dx.m == 8 || dx.m == 16) && std::max(kk, k) <= 1024 &&
+           !(flags & GBIVF_TABLE_DIRECT);
+}
+
+// GBIVF_MIXED_SCAN_AUTO -> GBIVF_MIXED_SCAN or nothing
+unsigned resolve_scan_form(const gbivf_index* ix, unsigned flags, int k, int kl) {
+    if (!(flags & GBIVF_MIXED_SCAN_AUTO)) return flags;
+    flags &= ~GBIVF_MIXED_SCAN_AUTO;
+    const bool want = ix->auto_tuned ? ix->auto_mixed : ix->dx.m == 16;
+    return want && mixed_scan_applies(ix->dx, k, kl, flags) ? flags | GBIVF_MIXED_SCAN : flags;
+}
+
 int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl, int w, unsigned flags,
                        int32_t* d_ids, float* d_dis, cudaStream_t st, const int32_t* d_w = nullptr,
                        const int32_t* d_k = nullptr, const int64_t* d_off = nullptr) {
     if (nq == 0) return GBIVF_OK;
+    flags = resolve_scan_form(ix, flags, k, kl);
     const DevIndex& dx = ix->dx;
     CK(ix->w_qn.ensure(sizeof(double) * nq));
     CK(ix->w_coaidx.ensure(sizeof(int32_t) * (size_t)nq * w));
@@ -965,81 +985,125 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
     if (nq <= 0 || !d_queries) return fail(GBIVF_ERR_INVALID, "empty calibration batch");
     std::lock_guard<std::mutex> lk(ix->mu);
     DeviceGuard g(ix->device);
+    // GBIVF_MIXED_SCAN_AUTO: the kernel variant is tuned on the exact form, then the two scan forms
+    // are timed with it and the faster one is kept for the flag
+    const bool auto_form = flags & GBIVF_MIXED_SCAN_AUTO;
     const std::string key = tune_key(ix, k, w, flags);
+    const std::string form_key = key + "_scanform";
+    flags &= ~GBIVF_MIXED_SCAN_AUTO;
     const char* cache = getenv("GBIVF_TUNE_CACHE");
-    if (cache) {  // "key threads" lines; threads 0 = the general kernel
+    int cached_th = -1, cached_form = -1;
+    if (cache) {  // "key threads" lines (threads 0 = the general kernel) and "key_scanform 0|1" lines
         if (FILE* f = fopen(cache, "r")) {
             char kbuf[600];
-            int th = -1;
-            while (fscanf(f, "%599s %d", kbuf, &th) == 2) {
-                if (key == kbuf) {
-                    ix->use_persistent = th != 0;
-                    ix->scan_threads = th == 1024 ? 1024 : 512;
-                    if (choice) *choice = th;
-                    if (times_ms) times_ms[0] = times_ms[1] = times_ms[2] = -1.0f;
-                    fclose(f);
-                    return GBIVF_OK;
-                }
+            int v = -1;
+            while (fscanf(f, "%599s %d", kbuf, &v) == 2) {
+                if (key == kbuf) cached_th = v;
+                if (form_key == kbuf) cached_form = v;
             }
             fclose(f);
+        }
+    }
+    if (cached_th >= 0) {
+        ix->use_persistent = cached_th != 0;
+        ix->scan_threads = cached_th == 1024 ? 1024 : 512;
+        if (choice) *choice = cached_th;
+        if (times_ms) times_ms[0] = times_ms[1] = times_ms[2] = -1.0f;
+        if (!auto_form) return GBIVF_OK;
+        if (cached_form >= 0) {
+            ix->auto_tuned = true;
+            ix->auto_mixed = cached_form != 0;
+            return GBIVF_OK;
         }
     }
     const size_t ob = (size_t)nq * k;
     CK(ix->w_ids.ensure(sizeof(int32_t) * ob));
     CK(ix->w_dis.ensure(sizeof(float) * ob));
     CK(ix->w_queue.ensure(sizeof(int)));
-    const bool save_p = ix->use_persistent;
-    const int save_t = ix->scan_threads;
-    float best = 1e30f;
-    int best_i = -1;
-    for (int i = 0; i < 3; i++) {
-        ix->use_persistent = kVariants[i].persistent;
-        ix->scan_threads = kVariants[i].persistent ? kVariants[i].threads : save_t;
-        float t = -1.0f;
-        ScanArgs probe;
-        probe.nq = nq;
-        probe.w = w;
-        probe.k = k;
-        probe.kl = kl;
-        probe.flags = flags & GBIVF_RERANK ? SCAN_RERANK : 0;
-        probe.queue = ix->w_queue.as<int>();
-        const bool applies = !kVariants[i].persistent || scan_persistent_supported(ix->dx, probe);
-        if (applies) {
-            float sum = 0.0f;
-            for (int rep = 0; rep < 3 && rc == GBIVF_OK; rep++) {
-                rc = search_device_impl(ix, d_queries, nq, k, kl, w, flags | GBIVF_PROFILE, ix->w_ids.as<int32_t>(),
-                                        ix->w_dis.as<float>(), ix->stream);
+    // scan + finalize time of one search, the mean of repetitions 2 and 3
+    auto time_scan = [&](unsigned fl, float* out) -> int {
+        float sum = 0.0f;
+        for (int rep = 0; rep < 3; rep++) {
+            int r = search_device_impl(ix, d_queries, nq, k, kl, w, fl | GBIVF_PROFILE, ix->w_ids.as<int32_t>(),
+                                       ix->w_dis.as<float>(), ix->stream);
+            if (r) return r;
+            CK(cudaStreamSynchronize(ix->stream));
+            float sm = 0;
+            CK(cudaEventElapsedTime(&sm, ix->ev[1], ix->ev[2]));
+            if (rep > 0) sum += sm;
+        }
+        *out = sum / 2.0f;
+        return GBIVF_OK;
+    };
+    if (cached_th < 0) {
+        const bool save_p = ix->use_persistent;
+        const int save_t = ix->scan_threads;
+        float best = 1e30f;
+        int best_i = -1;
+        for (int i = 0; i < 3; i++) {
+            ix->use_persistent = kVariants[i].persistent;
+            ix->scan_threads = kVariants[i].persistent ? kVariants[i].threads : save_t;
+            float t = -1.0f;
+            ScanArgs probe;
+            probe.nq = nq;
+            probe.w = w;
+            probe.k = k;
+            probe.kl = kl;
+            probe.flags = flags & GBIVF_RERANK ? SCAN_RERANK : 0;
+            probe.queue = ix->w_queue.as<int>();
+            const bool applies = !kVariants[i].persistent || scan_persistent_supported(ix->dx, probe);
+            if (applies) {
+                rc = time_scan(flags, &t);
                 if (rc) break;
-                CK(cudaStreamSynchronize(ix->stream));
-                float cm = 0, sm = 0;
-                CK(cudaEventElapsedTime(&cm, ix->ev[0], ix->ev[1]));
-                CK(cudaEventElapsedTime(&sm, ix->ev[1], ix->ev[2]));
-                if (rep > 0) sum += sm;
+                if (t < best) {
+                    best = t;
+                    best_i = i;
+                }
             }
-            if (rc) break;
-            t = sum / 2.0f;
-            if (t < best) {
-                best = t;
-                best_i = i;
+            if (times_ms) times_ms[i] = t;
+        }
+        ix->mixed_pending = false;
+        if (rc || best_i < 0) {
+            ix->use_persistent = save_p;
+            ix->scan_threads = save_t;
+            return rc ? rc : fail(GBIVF_ERR_INVALID, "no scan kernel applies");
+        }
+        ix->use_persistent = kVariants[best_i].persistent;
+        ix->scan_threads = kVariants[best_i].persistent ? kVariants[best_i].threads : save_t;
+        const int th = kVariants[best_i].persistent ? kVariants[best_i].threads : 0;
+        if (choice) *choice = th;
+        if (cache)
+            if (FILE* f = fopen(cache, "a")) {
+                fprintf(f, "%s %d\n", key.c_str(), th);
+                fclose(f);
             }
-        }
-        if (times_ms) times_ms[i] = t;
     }
-    ix->mixed_pending = false;
-    if (rc || best_i < 0) {
-        ix->use_persistent = save_p;
-        ix->scan_threads = save_t;
-        return rc ? rc : fail(GBIVF_ERR_INVALID, "no scan kernel applies");
-    }
-    ix->use_persistent = kVariants[best_i].persistent;
-    ix->scan_threads = kVariants[best_i].persistent ? kVariants[best_i].threads : save_t;
-    const int th = kVariants[best_i].persistent ? kVariants[best_i].threads : 0;
-    if (choice) *choice = th;
-    if (cache)
-        if (FILE* f = fopen(cache, "a")) {
-            fprintf(f, "%s %d\n", key.c_str(), th);
-            fclose(f);
+    if (auto_form) {
+        bool mixed = false;
+        if (mixed_scan_applies(ix->dx, k, kl, flags)) {
+            float t_exact = 0.0f, t_mixed = 0.0f;
+            if ((rc = time_scan(flags, &t_exact)) || (rc = time_scan(flags | GBIVF_MIXED_SCAN, &t_mixed))) {
+                ix->mixed_pending = false;
+                return rc;
+            }
+            mixed = t_mixed < t_exact;
         }
+        ix->mixed_pending = false;
+        ix->auto_tuned = true;
+        ix->auto_mixed = mixed;
+        if (cache)
+            if (FILE* f = fopen(cache, "a")) {
+                fprintf(f, "%s %d\n", form_key.c_str(), mixed ? 1 : 0);
+                fclose(f);
+            }
+    }
+    return GBIVF_OK;
+}
+
+int gbivf_index_scan_form(const gbivf_index* ix, int* tuned, int* mixed) {
+    if (!ix || !tuned || !mixed) return fail(GBIVF_ERR_INVALID, "NULL argument");
+    *tuned = ix->auto_tuned ? 1 : 0;
+    *mixed = (ix->auto_tuned ? ix->auto_mixed : ix->dx.m == 16) ? 1 : 0;
     return GBIVF_OK;
 }
 

@@ -106,6 +106,19 @@ class GpuIndex:
         return d.value, c.value, m.value, ks.value, n.value
 
     # -- searches ---------------------------------------------------------
+    @staticmethod
+    def _scan_flag(mixed_scan):
+        """mixed_scan: False (exact form), True (precision form) or "auto" (the engine's choice)."""
+        if mixed_scan == "auto":
+            return _lib.GBIVF_MIXED_SCAN_AUTO
+        return _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+
+    def scan_form(self):
+        """(tuned, mixed): the scan form mixed_scan="auto" resolves to on this index."""
+        t, m = C.c_int(), C.c_int()
+        check(self.lib.gbivf_index_scan_form(self.h, C.byref(t), C.byref(m)))
+        return bool(t.value), bool(m.value)
+
     def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False,
                mixed_scan=False, refine=False):
         """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
@@ -121,7 +134,7 @@ class GpuIndex:
             assert dis.shape == (nq, k) and dis.dtype == np.float32 and dis.flags.c_contiguous
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_TABLE_DIRECT if direct else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
-        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
@@ -132,7 +145,7 @@ class GpuIndex:
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
-        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
@@ -148,7 +161,7 @@ class GpuIndex:
         np.cumsum(kq, out=off[1:])
         ids = np.empty(int(off[-1]), np.int32)
         dis = np.empty(int(off[-1]), np.float32)
-        flags = (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0) | (_lib.GBIVF_MIXED_SCAN if mixed_scan else 0)
+        flags = (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0) | self._scan_flag(mixed_scan)
         check(self.lib.gbivf_search_batched(self.h, _p(q), q.shape[0], _p(wq), _p(kq), flags, _p(ids), _p(dis)))
         return ids, dis, off
 
@@ -157,7 +170,7 @@ class GpuIndex:
                       refine=False):
         """Capture a device-buffer search as a CUDA graph (see gbivf_graph_capture)."""
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
-        flags |= _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
+        flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
         g = C.c_void_p()
         check(self.lib.gbivf_graph_capture(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
@@ -166,9 +179,11 @@ class GpuIndex:
                                            C.byref(g)))
         return SearchGraph(self.lib, g)
 
-    def autotune(self, d_queries_ptr, nq, k, w, kl=None, rerank=False, mixed_coarse=False):
-        """Pick the fastest scan kernel for this index; returns (choice, times_ms)."""
+    def autotune(self, d_queries_ptr, nq, k, w, kl=None, rerank=False, mixed_coarse=False, scan_form=False):
+        """Pick the fastest scan kernel for this index; returns (choice, times_ms). With
+        scan_form=True also time both scan forms for mixed_scan="auto" (see scan_form())."""
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
+        flags |= _lib.GBIVF_MIXED_SCAN_AUTO if scan_form else 0
         ch = C.c_int()
         t = (C.c_float * 3)()
         check(self.lib.gbivf_index_autotune(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,

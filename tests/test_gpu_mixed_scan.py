@@ -129,3 +129,42 @@ def test_mixed_scan_long_lists_every_shape(long_list_indexes, m, threads, monkey
         assert ok, "a returned distance differs from the plain form's"
         assert same >= 0.99
     gi.close()
+
+
+@pytest.mark.parametrize("m", [8, 16])
+def test_auto_scan_form_default_then_tuned(long_list_indexes, m):
+    """mixed_scan="auto" returns exactly what the form it resolves to returns: before tuning the
+    precision form when m = 16 and the exact form otherwise; after the autotuner timed both forms,
+    the faster one (reported by scan_form()). Combined with an explicit form it is rejected."""
+    import torch
+
+    from mestrado_gb300.engine import GbivfError, GpuIndex
+
+    ixs, q = long_list_indexes
+    gi = GpuIndex(ixs[m])
+    k, w = 50, 6
+    exact = gi.search(q, k, w)
+    mixed = gi.search(q, k, w, mixed_scan=True)
+
+    def same(a, b):
+        return np.array_equal(a[0], b[0]) and np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+
+    assert gi.scan_form() == (False, m == 16)
+    assert same(gi.search(q, k, w, mixed_scan="auto"), mixed if m == 16 else exact)
+    d_q = torch.from_numpy(q).cuda()
+    gi.autotune(d_q.data_ptr(), len(q), k, w, scan_form=True)
+    tuned, form_mixed = gi.scan_form()
+    print(f"m={m}: tuned scan form {'precision' if form_mixed else 'exact'}")
+    assert tuned
+    assert same(gi.search(q, k, w, mixed_scan="auto"), mixed if form_mixed else exact)
+    ids, dis, off = gi.search_batched(q, np.full(len(q), w, np.int32), np.full(len(q), k, np.int32),
+                                      mixed_scan="auto")
+    ref = mixed if form_mixed else exact
+    np.testing.assert_array_equal(ids.reshape(len(q), k), ref[0])
+    from mestrado_gb300._lib import GBIVF_MIXED_SCAN, GBIVF_MIXED_SCAN_AUTO, check
+
+    with pytest.raises(GbivfError) as e:
+        check(gi.lib.gbivf_ivfpq_search(gi.h, q.ctypes.data, len(q), k, k, w, GBIVF_MIXED_SCAN | GBIVF_MIXED_SCAN_AUTO,
+                                        ids.ctypes.data, dis.ctypes.data))
+    assert e.value.code == 1
+    gi.close()
