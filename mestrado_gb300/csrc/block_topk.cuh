@@ -106,6 +106,35 @@ __device__ __forceinline__ void topk_push_rows(TopKSmem& s, const u64 (&key)[R],
     }
 }
 
+// Ascending order of n unique keys a[0..n) (with their ids b[0..n) when b is not NULL), for
+// n <= 2 * blockDim.x: every element's final position is the number of smaller keys, found by one
+// pass over the keys; two block barriers in all, where a bitonic network of n = 128 takes 28.
+__device__ inline void rank_sort(u64* a, int32_t* b, int n) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const bool h0 = tid < n, h1 = tid + nt < n;
+    u64 k0 = h0 ? a[tid] : KEY_MAX, k1 = h1 ? a[tid + nt] : KEY_MAX;
+    int32_t i0 = 0, i1 = 0;
+    if (b) {
+        if (h0) i0 = b[tid];
+        if (h1) i1 = b[tid + nt];
+    }
+    int r0 = 0, r1 = 0;
+    if (h0)
+        for (int j = 0; j < n; j++) {
+            const u64 x = a[j];
+            r0 += x < k0;
+            r1 += x < k1;
+        }
+    __syncthreads();
+    if (h0) a[r0] = k0;
+    if (h1) a[r1] = k1;
+    if (b) {
+        if (h0) b[r0] = i0;
+        if (h1) b[r1] = i1;
+    }
+    __syncthreads();
+}
+
 __device__ inline void bitonic_sort_smem(u64* a, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int size = 2; size <= n; size <<= 1) {

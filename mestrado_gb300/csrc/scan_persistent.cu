@@ -560,6 +560,9 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
 // one candidate per thread), 512 for the refinement re-rank of the exact form (eight lanes per
 // candidate)
 constexpr int FIN_NT = 128;
+// finalize sets of at most this many keys are ordered by rank_sort (one pass over the keys per
+// element, two barriers), larger ones by a bitonic network (log^2 barriers, fewer operations)
+constexpr int RANK_SORT_MAX = 256;
 constexpr int FIN_NT_BIG = 512;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
@@ -729,10 +732,12 @@ __global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
             keys[c] = key;
         }
         __syncthreads();
-        bitonic_sort_pairs(keys, ids, p2);
+        if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);  // (the KEY_MAX padding stays past n)
+        else bitonic_sort_pairs(keys, ids, p2);
         n = min(n, (rerank || refine) ? a.kl : query_k(a, q));
     } else {
-        bitonic_sort_pairs(keys, ids, p2);
+        if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);
+        else bitonic_sort_pairs(keys, ids, p2);
     }
     auto base_id = [&](int c) { return slots ? ix.ids[a.cand_id[hb + ids[c]]] : ids[c]; };
     const float inf = __int_as_float(0x7f800000);
@@ -786,7 +791,8 @@ __global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
         keys[c] = key;  // (ids[] keeps the ADC order the payload refers to)
     }
     __syncthreads();
-    bitonic_sort_smem(keys, pr);
+    if (n <= RANK_SORT_MAX) rank_sort(keys, nullptr, n);
+    else bitonic_sort_smem(keys, pr);
     const int kq = query_k(a, q);
     const int64_t o = query_out(a, q);
     const int kr = min(kq, n);
