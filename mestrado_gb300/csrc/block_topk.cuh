@@ -301,7 +301,9 @@ __device__ __forceinline__ void topk_finish(TopKSmem& s) {
     __syncthreads();
     topk_flush(s, nb);
     const int n = *s.nbest;
-    if (n > 1) {
+    if (n > 1 && n <= 256 && n <= 2 * (int)blockDim.x) {
+        rank_sort(s.best, nullptr, n);  // (the flush's last barrier published the best set)
+    } else if (n > 1) {
         int p = 2;
         while (p < n) p <<= 1;
         for (int i = n + threadIdx.x; i < p; i += blockDim.x) s.best[i] = KEY_MAX;
