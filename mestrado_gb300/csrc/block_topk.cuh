@@ -11,7 +11,8 @@
 //     block radix select (8-bit digits, starting at the highest bit in which
 //     the pool's keys differ), keeps the keys <= it as the new best set
 //     (unordered) and lowers the threshold to it;
-//   * the final call sorts the k survivors (bitonic network).
+//   * the final call sorts the k survivors (by rank up to 256 keys, else a
+//     bitonic network).
 //
 // Keys are unique (the low 32 bits carry a unique payload), so the result is
 // exactly the k smallest keys, ascending.
