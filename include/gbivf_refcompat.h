@@ -60,14 +60,17 @@ typedef struct ivf {
 } ivf_t;
 
 /* ivfpq_search: w probes, ADC k-min of kl, exact re-rank of those kl against
- * vbase to k; ids nq x k. The index (ivf) is uploaded to the GPU on the first
- * call with a given ivf pointer and reused after that; vbase likewise. */
+ * vbase to k; ids nq x k. The index (ivfpq + ivf) and vbase stay on the GPU
+ * between calls while their contents are unchanged: every call fingerprints
+ * their bytes (one pass over them) and uploads again on any change, because
+ * the reference's ivfpq_assign returns the same static ivf array each time
+ * (sequential/ivf_pq/ivf_assign.cpp:19). */
 void ivfpq_search(ivfpq_t ivfpq, ivf_t *ivf, mat vquery, mat vbase, int k, int kl, int w, int *ids,
                   float *dis);
 
 /* pq_search: exhaustive ADC over the codebook; dis and ids k x nq
- * column-major, ids 1-based. The codebook is uploaded on the first call with
- * a given codebook.mat pointer. */
+ * column-major, ids 1-based. The codes and centroids stay on the GPU between
+ * calls while their contents (fingerprinted on every call) are unchanged. */
 void pq_search(pqtipo pq, matI codebook, mat vquery, int k, float *dis, int *ids);
 
 #endif
