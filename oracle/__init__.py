@@ -103,6 +103,26 @@ def ivfpq_search(ix, queries, k, w, kl=None, base=None, rerank=True, ties=TIES_H
     return (ids, dis, *st) if stages else (ids, dis)
 
 
+def search_batched(ix, queries, w_per_q, k_per_q, ties=TIES_KEYED, nthreads=1):
+    """The engine's uneven batch (gbivf_search_batched) restated: per-query nprobe and k, no
+    re-rank. Returns (ids, dis, offsets): query q's results are ids[offsets[q]:offsets[q+1]]."""
+    q = _c(queries, np.float32)
+    wq = _c(w_per_q, np.int32)
+    kq = _c(k_per_q, np.int32)
+    off = np.zeros(len(kq) + 1, np.int64)
+    np.cumsum(kq, out=off[1:])
+    ids = np.empty(int(off[-1]), np.int32)
+    dis = np.empty(int(off[-1]), np.float32)
+    s, keep = _pin(ix)
+    lib().orc_ivfpq_search_batched.restype = C.c_int
+    rc = lib().orc_ivfpq_search_batched(C.byref(s), _ptr(q), C.c_int(q.shape[0]), _ptr(wq), _ptr(kq),
+                                        _ptr(off), C.c_int(ties), _ptr(ids), _ptr(dis), C.c_int(nthreads))
+    del keep
+    if rc != 0:
+        raise RuntimeError(f"orc_ivfpq_search_batched failed ({rc})")
+    return ids, dis, off
+
+
 def pq_search(d, m, ks, pq, codes, queries, k, nthreads=1):
     """Restated pq_search: column-major (k x nq) dis and 1-based ids."""
     q = _c(queries, np.float32)

@@ -20,6 +20,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# Where the reference tree lies: MESTRADO_REFERENCE, else the mount of the build container. This recipe
+# is the one file that names it; on a machine without the tree (the GPU host) nothing is built from it.
 REF_ROOT = os.environ.get("MESTRADO_REFERENCE", "/root/reference")
 REF_SEQ = os.path.join(REF_ROOT, "sequential")
 LIB = os.path.join(HERE, "liboracle.so")

@@ -453,6 +453,80 @@ int orc_ivfpq_search(const orc_index *ix, const float *queries, int nq,
     return err;
 }
 
+/* The uneven batch of the engine's gbivf_search_batched, restated per query
+ * with the same steps as orc_ivfpq_search (no re-rank): query q probes its
+ * w_per_q[q] nearest lists and keeps its k_per_q[q] best ADC candidates,
+ * written at out_off[q] (ids -1 / distances +inf past L_q). */
+int orc_ivfpq_search_batched(const orc_index *ix, const float *queries, int nq,
+                             const int32_t *w_per_q, const int32_t *k_per_q,
+                             const int64_t *out_off, int ties, int32_t *ids,
+                             float *dis, int nthreads) {
+    if (check_index(ix) || nq < 0) return -1;
+    for (int q = 0; q < nq; q++)
+        if (w_per_q[q] <= 0 || w_per_q[q] > ix->coarsek || k_per_q[q] <= 0) return -1;
+    orc_pre pre;
+    if (pre_init(ix, &pre)) return -2;
+    const int d = ix->d, C = ix->coarsek;
+    int err = 0;
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (int q = 0; q < nq; q++) {
+        const int w = w_per_q[q], k = k_per_q[q];
+        const float *x = queries + (long)q * d;
+        float *cd = (float *)malloc(sizeof(float) * C);
+        int *qco = (int *)malloc(sizeof(int) * w);
+        float *qcd = (float *)malloc(sizeof(float) * w);
+        float *r = (float *)malloc(sizeof(float) * d);
+        float *tab = (float *)malloc(sizeof(float) * ix->m * ix->ks);
+        if (!cd || !qco || !qcd || !r || !tab) {
+            err = -2;
+            free(cd); free(qco); free(qcd); free(r); free(tab);
+            continue;
+        }
+        double xn = norm_d(x, d);
+        for (int c = 0; c < C; c++)
+            cd[c] = expansion_dist(pre.coa_norm[c], xn, ix->coa + (long)c * d, x, d);
+        select_k(cd, C, w, ties, qco, qcd);
+        long L = 0;
+        for (int j = 0; j < w; j++)
+            if (qco[j] >= 0) L += ix->list_off[qco[j] + 1] - ix->list_off[qco[j]];
+        float *qdis = (float *)malloc(sizeof(float) * (L > 0 ? L : 1));
+        int32_t *qid = (int32_t *)malloc(sizeof(int32_t) * (L > 0 ? L : 1));
+        long pos = 0;
+        for (int j = 0; j < w; j++) {
+            int l = qco[j];
+            if (l < 0) continue;
+            const float *cen = ix->coa + (long)l * d;
+            for (int i = 0; i < d; i++) r[i] = x[i] - cen[i];
+            build_table(ix, &pre, r, ORC_TABLE_EXPANSION, tab);
+            long beg = ix->list_off[l], n = ix->list_off[l + 1] - beg;
+            adc_scan(ix, tab, beg, n, qdis + pos);
+            memcpy(qid + pos, ix->ids + beg, sizeof(int32_t) * n);
+            pos += n;
+        }
+        int kt = (int)(L < k ? L : k);
+        int *sel = (int *)malloc(sizeof(int) * (kt > 0 ? kt : 1));
+        orc_k_min(qdis, (int)L, kt, sel);
+        const long o = (long)out_off[q];
+        for (int c = 0; c < k; c++) {
+            ids[o + c] = c < kt ? qid[sel[c]] : -1;
+            dis[o + c] = c < kt ? qdis[sel[c]] : INFINITY;
+        }
+        free(sel);
+        free(qdis);
+        free(qid);
+        free(cd);
+        free(qco);
+        free(qcd);
+        free(r);
+        free(tab);
+    }
+    pre_free(&pre);
+    return err;
+}
+
 int orc_pq_search(int d, int m, int ks, const float *pq, const uint8_t *codes,
                   int64_t n, const float *queries, int nq, int k, float *dis,
                   int32_t *ids, int nthreads) {

@@ -86,6 +86,12 @@ int orc_pq_search(int d, int m, int ks, const float *pq, const uint8_t *codes,
  * (nres x d, nres = nq*w) and rid_to_ivf: direct-sum tables, ADC scan and
  * an exact top-k per query, written packed at qid_to_starting_outid,
  * ascending by (distance, position). */
+/* uneven batch (per-query nprobe and k, packed outputs at out_off[q]), no re-rank */
+int orc_ivfpq_search_batched(const orc_index *ix, const float *queries, int nq,
+                             const int32_t *w_per_q, const int32_t *k_per_q,
+                             const int64_t *out_off, int ties, int32_t *ids,
+                             float *dis, int nthreads);
+
 int orc_core_cpu(const orc_index *ix, const float *residual, int nres,
                  const int32_t *rid_to_ivf, const int32_t *qid_to_starting_outid,
                  int32_t *idxs, float *dists, int k, int w, int nthreads);

@@ -14,9 +14,10 @@ import numpy as np
 import pytest
 
 from mestrado_gb300 import build as engine_build
+from oracle import build as oracle_build
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SEQ = os.path.join(os.environ.get("MESTRADO_REFERENCE", "/root/reference"), "sequential")
+REF_SEQ = oracle_build.REF_SEQ  # the reference tree's location is known to the oracle's build recipe only
 SEQ_SYMS = ["_Z12ivfpq_search5ivfpqP3ivf3matS2_iiiPiPf", "_Z9pq_search6pqtipo4matI3matiPfPi"]
 PAR2_SYMS = ["_Z8core_gpu6pqtipo3matP3ivfiPiS3_4matIS0_ii", "_Z19preallocate_gpu_mem6pqtipoP3ivfi",
              "_Z18deallocate_gpu_memv"]
