@@ -1,34 +1,51 @@
 #!/usr/bin/env python
-"""Benchmark of the IVF-PQ search path (ivfpq_search drop-in) on GB300.
+"""Benchmark of the IVF-PQ search path (the reference's ivfpq_search and its
+batched GPU replacement) on GB300.
 
-Workload (default ``--config cfg2``): plain FP32 ivfpq_search over a 1M-vector
-index -- base 1,000,000 x d=128 from a 1,024-component Gaussian mixture
-(means U[0,120], sigma 20, clipped to [0,255], rounded; seed 0), 100,000
-training vectors, C = 1,024 lists, m = 8 x 256 codes, 10,000 queries per
-step, w = 16 probes, k = 100, re-rank of kl = 100 ADC candidates.
-The synthetic mixture stands in for the reference's SIFT runs.
+Headline (default, ``--config cfg4``): the workload the metric is quoted on --
+batched search of 32,768 queries over a 100M-vector index (d = 128,
+Zipf(1.1)-sized mixture components, C = 262,144 lists, m = 16 x 256 codes),
+each query with its own nprobe (log-uniform in 1..256) and k (from
+{1, 10, 100, 1000}), in two forms:
 
-A step is one search of the whole 10,000-query batch.
+* plain: FP32 throughout, the reference's arithmetic (the drop-in);
+* mixed: BF16 tensor-core coarse stage with an FP32 re-check of every
+  centroid within the error margin (the same probe lists), FP16 PQ tables
+  summed in FP32 with the 4k best re-scored exactly (the same ids).
 
-* ``value``: QPS with queries, index and outputs resident in HBM, CUDA
-  events around each step on the launching stream, L2 flushed (a 256 MB
-  write) between steps outside the timed events.
-* ``e2e``: QPS through the host C ABI call (gbivf_ivfpq_search): queries
-  copied from pinned host memory, ids and distances copied back, per step.
-* ``roofline``: the fused scan kernel (ivf_scan_kernel) -- algorithmic bytes
-  = sum over queries of the probed lists' code bytes (n_l * m) divided by
-  the kernel's CUDA-event time, against the measured HBM copy bandwidth.
-* ``cpu_baseline``: the CPU oracle (plain-C restatement of the reference's
-  ivfpq_search) on the host cores, OpenMP over queries.
+A step is one search of the whole batch, replayed as a CUDA graph.
 
-``--impl reference`` times that CPU implementation alone, in steps of a
-bounded sample of the same queries.
+* ``value``: mixed-form QPS with queries, index and outputs resident in HBM,
+  CUDA events around each replay on the launching stream, L2 flushed (a 256 MB
+  write) between steps outside the timed events; ``forms`` holds both forms,
+  their ratio and recall@100 (equal by construction: identical ids).
+* ``e2e``: the same batch through the host C ABI (gbivf_search_batched):
+  queries, nprobe and k copied from pinned host memory, ids and distances
+  copied back, per step.
+* ``roofline``: the dominant kernel of the mixed step (the ADC scan):
+  algorithmic bytes (sum over queries of the probed lists' codes, n_l * m)
+  over its CUDA-event time, against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the CPU oracle (the plain-C restatement of the
+  reference's search) on all host cores, on a sample of the same queries.
+* ``parity``: the plain form against the oracle on a sample of queries (ids
+  and distance bits), the mixed form against the plain form on all queries.
+* ``sub``: the 1M drop-in workload (``ivfpq_search`` with re-rank, all
+  10,000 queries checked against the oracle, the reference's OpenMP
+  ``core_cpu`` timed) and the 10M workload (C = 65,536, w = 32, k = 100).
+
+``--impl reference`` times the oracle alone on the headline workload, in
+steps of a bounded sample of its queries, with every host thread. The index
+it searches is built by the engine's GPU index builder (input preparation;
+nothing of the engine runs in its timed region).
+
+The synthetic mixture stands in for the reference's SIFT/BIGANN runs.
 """
 from __future__ import annotations
 
 import argparse
 import hashlib
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -40,6 +57,10 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+METRIC = "QPS at equal recall@100, batched mixed-prec vs plain FP32 GPU; ADC scan GB/s"
+HEADLINE = "cfg4"
+
+# Host-built indexes: the drop-in workloads of the reference's own CPU runs.
 CONFIGS = {
     "cfg2": dict(d=128, ncomp=1024, seed=0, nbase=1_000_000, ntrain=100_000, nq=10_000, C=1024, m=8,
                  w=16, k=100, kl=100, rerank=True, train_iters=10),
@@ -55,8 +76,7 @@ LARGE = {
     "cfg5": dict(d=128, ncomp=16384, seed=0, zipf=None, nbase=1_000_000_000, ntrain=2_621_440, nq=10_000,
                  C=262144, m=8, m2=8, w=64, k=100, kl=1000, uneven=False, train_iters=6, recall_q=100,
                  stream=True),
-    # the 100M workload's shape at 1/5 scale (20M base, 65,536 Zipf lists, m = 16, uneven nprobe / k):
-    # small enough to profile with every ncu section
+    # the 100M workload's shape at 1/5 scale (20M base, 65,536 Zipf lists, m = 16, uneven nprobe / k)
     "cfg4s": dict(d=128, ncomp=65536, seed=0, zipf=1.1, nbase=20_000_000, ntrain=655_360, nq=8192,
                   C=65536, m=16, w=256, k=1000, uneven=True, train_iters=4, recall_q=256),
     # 10M base, 4,096-component mixture, 65,536 lists, m = 8, 10k queries, w = 32, k = 100
@@ -78,8 +98,27 @@ def workload_name(c):
             f"rerank kl={c['kl']}")
 
 
+def large_workload(name, c):
+    return (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture"
+            f"{', Zipf ' + str(c['zipf']) + ' component sizes' if c['zipf'] else ''}), C={c['C']:,} lists, "
+            f"m={c['m']}x256, {c['nq']:,} queries/step, "
+            + (f"nprobe log-uniform 1..{c['w']}, k in {{1,10,100,1000}}" if c["uneven"] else f"w={c['w']}, k={c['k']}"))
+
+
+def large_config(name, c):
+    """The config dict of a large workload: the same in the engine's arm and the reference arm."""
+    return {"workload": large_workload(name, c), "queries_per_step": c["nq"],
+            "l2": "flushed between steps (256 MB write)",
+            "index": "built on the GPU by the engine's index builder (k-means with FP64 centroid sums, PQ "
+                     "training and encoding); input preparation, outside every timed region"}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def ncpu():
+    return os.cpu_count() or 1
 
 
 # ---------------------------------------------------------------------------
@@ -87,7 +126,7 @@ def log(*a):
 # ---------------------------------------------------------------------------
 
 def make_inputs(c, rank=0):
-    """(index data, base, queries): cached on local disk by config."""
+    """(index data, base, queries): host-built, cached on local disk by config."""
     from mestrado_gb300.ivfdata import IVFPQData
     from mestrado_gb300.synth import STREAM_QUERY, Mixture
     from mestrado_gb300.train import build_index
@@ -111,6 +150,51 @@ def make_inputs(c, rank=0):
         os.replace(tmp, ipath)
         log(f"index built in {time.time() - t:.1f}s")
     return ix, base, queries, key
+
+
+def large_inputs(name, c, dev, rank=0, dist=None):
+    """(GPU mixture, host index, device queries, build seconds or None): the index is built on the
+    GPU once per machine and cached on local disk (rank 0 builds, the other ranks wait and load)."""
+    import torch
+
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
+    from mestrado_gb300.ivfdata import IVFPQData
+    from mestrado_gb300.synth import Mixture
+
+    gm = GpuMixture(Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"], zipf=c["zipf"]), device=dev)
+    key = hashlib.sha1(json.dumps({k: c[k] for k in sorted(c)}, sort_keys=True).encode()).hexdigest()[:12]
+    path = os.path.join(CACHE, f"{name}_{key}")
+    t_build, ix = None, None
+    if rank == 0 and not os.path.isdir(path):
+        t0 = time.time()
+        base = gm.generate(c["nbase"], stream_id=1)
+        train = gm.generate(c["ntrain"], stream_id=2)
+        ix = build_index_gpu(base, train, c["C"], c["m"], niter=c["train_iters"], seed=c["seed"])
+        del base, train
+        torch.cuda.empty_cache()
+        t_build = time.time() - t0
+        os.makedirs(CACHE, exist_ok=True)
+        ix.save_dir(path)
+        sizes = ix.list_sizes()
+        log(f"{name}: index built in {t_build:.1f}s; lists {sizes.min()}..{sizes.max()}")
+    if dist is not None:
+        dist.barrier()
+    if ix is None:
+        ix = IVFPQData.load_dir(path)
+    queries = gm.generate(c["nq"], stream_id=3, row0=rank * c["nq"])
+    return gm, ix, queries, t_build
+
+
+def batch_shape(c, nq):
+    """Per-query nprobe and k of a large workload (seeded; uniform where the workload is)."""
+    rng = np.random.default_rng(c["seed"] + 17)
+    if c["uneven"]:
+        wq = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(c["w"] + 1), nq))), 1, c["w"]).astype(np.int32)
+        kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
+    else:
+        wq = np.full(nq, c["w"], np.int32)
+        kq = np.full(nq, c["k"], np.int32)
+    return wq, kq
 
 
 def ground_truth(base, queries, k, key, device):
@@ -146,6 +230,20 @@ def recall_report(ids, gt, k):
     r_at = {f"R@{r}": float(np.mean([(gt[i, 0] in ids[i, :r]) for i in range(len(ids))])) for r in (1, 10, 100)
             if r <= ids.shape[1]}
     return {f"recall@{k}": float(hits.mean() / k), **r_at}
+
+
+def packed_recall(ids, off, kq, gt, nsample):
+    """recall@k_q per query (k_q its own k) and recall@100 over the queries with k_q >= 100 (their
+    first 100 results against the 100 exact nearest), on the first nsample queries."""
+    at_k, at_100 = [], []
+    for i in range(nsample):
+        row = ids[off[i]:off[i] + kq[i]]
+        at_k.append(len(set(row[row >= 0].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i])
+        if kq[i] >= 100:
+            r = row[:100]
+            at_100.append(len(set(r[r >= 0].tolist()) & set(gt[i, :100].tolist())) / 100)
+    return {"recall@k": float(np.mean(at_k)) if at_k else None,
+            "recall@100": float(np.mean(at_100)) if at_100 else None, "recall@100_queries": len(at_100)}
 
 
 # ---------------------------------------------------------------------------
@@ -223,9 +321,10 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(config_name):
-    """DRAM bytes per scan-kernel launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"ivf_scan_{config_name}.txt")
+def profiled_traffic(name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary
+    profiles/<name>.txt, scaled there to a full launch of the workload (None if absent)."""
+    path = os.path.join(ROOT, "profiles", f"{name}.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch"):
@@ -236,7 +335,7 @@ def profiled_traffic(config_name):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (the oracle restatement of the reference, all host threads)
+# CPU baselines (the oracle: the plain-C restatement of the reference)
 # ---------------------------------------------------------------------------
 
 def cpu_search(ix, base, queries, c, nthreads, results=False):
@@ -247,6 +346,68 @@ def cpu_search(ix, base, queries, c, nthreads, results=False):
                                    nthreads=nthreads)
     t = time.perf_counter() - t
     return (t, ids, dis) if results else t
+
+
+def cpu_batched(ix, q, wq, kq, nthreads):
+    """(seconds, (ids, dis, off)) of the oracle's uneven batch."""
+    import oracle
+
+    t = time.perf_counter()
+    r = oracle.search_batched(ix, q, wq, kq, ties=oracle.TIES_KEYED, nthreads=nthreads)
+    return time.perf_counter() - t, r
+
+
+def sample_size(seconds_per_query, target_s, lo, hi):
+    return int(max(lo, min(hi, target_s / max(seconds_per_query, 1e-9))))
+
+
+def core_cpu_baseline(ix, queries, c):
+    """The reference's OpenMP CPU path, parallel2 core_cpu (parallel2/ivf_pq/ivf_search.cpp:61-117),
+    restated by the oracle: residuals and probe lists from the reference's coarse stage (knn_full then
+    bsxfunMINUS, timed separately on one thread), then core_cpu with its hard-coded team of 8 threads
+    (:62), and ceil(cores / 8) such calls at once on disjoint query slices."""
+    import concurrent.futures as cf
+
+    import oracle
+
+    w, k = c["w"], c["k"]
+    t0 = time.perf_counter()
+    coaidx, _ = oracle.knn_full(ix.coa, queries, w)
+    t_coarse = time.perf_counter() - t0
+    d = queries.shape[1]
+    res = np.ascontiguousarray((queries[:, None, :] - ix.coa[coaidx]).reshape(-1, d), np.float32)
+    rid = np.ascontiguousarray(coaidx.reshape(-1), np.int32)
+    cnt = np.minimum(ix.list_sizes()[coaidx].astype(np.int64).sum(1), k)
+    start = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int32)
+    nout = int(cnt.sum())
+    nq = len(queries)
+    oracle.core_cpu(ix, res[:w * 8], rid[:w * 8], start[:8], nout, k, w, nthreads=8)  # warm-up
+    t0 = time.perf_counter()
+    oracle.core_cpu(ix, res, rid, start, nout, k, w, nthreads=8)
+    t8 = time.perf_counter() - t0
+    ncalls = max(1, math.ceil(ncpu() / 8))
+    bounds = np.linspace(0, nq, ncalls + 1).astype(int)
+
+    def part(i):
+        a, b = bounds[i], bounds[i + 1]
+        st = start[a:b] - start[a] if b > a else start[a:b]
+        n = int(cnt[a:b].sum())
+        oracle.core_cpu(ix, res[a * w:b * w], rid[a * w:b * w], np.ascontiguousarray(st, np.int32), max(n, 1), k, w,
+                        nthreads=8)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(ncalls) as ex:
+        list(ex.map(part, range(ncalls)))
+    tn = time.perf_counter() - t0
+    return {"value": nq / t8, "unit": "queries/s", "cores": 8, "kind": "port",
+            "sample": f"{nq} queries: core_cpu with 8 OpenMP threads ({t8:.2f}s) on residuals from the "
+                      f"coarse stage",
+            "concurrent": {"value": nq / tn, "unit": "queries/s", "cores": 8 * ncalls, "calls": ncalls,
+                           "sample": f"{ncalls} concurrent core_cpu calls of 8 threads on disjoint slices "
+                                     f"({tn:.2f}s)"},
+            "coarse_stage": {"value": nq / t_coarse, "unit": "queries/s", "cores": 1,
+                             "sample": f"knn_full of {nq} queries over {ix.coarsek} centroids, one thread "
+                                       f"({t_coarse:.2f}s)"}}
 
 
 def parity_report(g_ids, g_dis, o_ids, o_dis):
@@ -275,32 +436,27 @@ def parity_report(g_ids, g_dis, o_ids, o_dis):
             "ties": "oracle in the reference's heap tie order; engine ties ordered by (distance, id)"}
 
 
-def run_reference(args, c, rank, world):
-    if rank != 0:
-        return
-    ix, base, queries, _ = make_inputs(c, 0)
-    nthreads = os.cpu_count() or 1
-    sample = min(len(queries), args.ref_sample)
-    qs = queries[:sample]
-    for _ in range(args.warmup):
-        cpu_search(ix, base, qs[: max(1, sample // 10)], c, nthreads)
-    ts = [cpu_search(ix, base, qs, c, nthreads) for _ in range(args.steps)]
-    total = sum(ts)
-    qps = sample * args.steps / total
-    line = {
-        "impl": "reference", "metric": "QPS", "value": qps, "unit": "queries/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": workload_name(c), "sample_queries_per_step": sample},
-        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{sample} of the {c['nq']} queries per step"},
-        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+def packed_parity(a_ids, a_dis, b_ids, b_dis, off, nq):
+    """Two packed result sets (query q at off[q]:off[q+1]) compared row by row: identical rows (ids
+    and distance bits), distance bits that differ for an id both return, and the share of real (not
+    padding) ids the rows have in common."""
+    same, mism, shared, real = 0, 0, 0, 0
+    for i in range(nq):
+        a, b = a_ids[off[i]:off[i + 1]], b_ids[off[i]:off[i + 1]]
+        ad, bd = a_dis[off[i]:off[i + 1]].view(np.uint32), b_dis[off[i]:off[i + 1]].view(np.uint32)
+        same += int(np.array_equal(a, b) and np.array_equal(ad, bd))
+        bm = dict(zip(b.tolist(), bd.tolist()))
+        mism += sum(int(x in bm and bm[x] != y) for x, y in zip(a.tolist(), ad.tolist()) if x >= 0)
+        ra, rb = set(a[a >= 0].tolist()), set(b[b >= 0].tolist())
+        shared += len(ra & rb)
+        real += max(len(ra), len(rb))
+    return {"queries": nq, "identical_rows_fraction": same / max(nq, 1), "distance_mismatches_on_shared_ids": mism,
+            "shared_real_ids_fraction": shared / max(real, 1),
+            "padding": "ids -1 (fewer candidates than k) are excluded from the id overlap"}
 
 
 # ---------------------------------------------------------------------------
-# GPU engine
+# multi-rank helpers
 # ---------------------------------------------------------------------------
 
 def max_over_ranks(x, dist, device):
@@ -320,25 +476,22 @@ def whole_job_rate(nq_per_rank, steps, world, seconds):
     return nq_per_rank * steps * world / seconds
 
 
-def run_gpu(args, c, rank, world, local_rank):
+# ---------------------------------------------------------------------------
+# the drop-in workload (host-built 1M index, ivfpq_search with re-rank)
+# ---------------------------------------------------------------------------
+
+def drop_in_record(args, c, rank, world, dist, dev, local_rank, with_cpu=True):
+    """QPS (device buffers), e2e (host buffers), roofline of the scan kernel, parity against the
+    oracle on every query, recall, and the CPU baselines of the drop-in workload."""
     import torch
 
     from mestrado_gb300.engine import GpuIndex
 
-    dev = torch.device("cuda", local_rank)
-    torch.cuda.set_device(dev)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
     ix_data, base, queries, key = make_inputs(c, rank)
     nq, k, kl, w, m = c["nq"], c["k"], c["kl"], c["w"], c["m"]
-
-    # CPU baseline first (rank 0, N=1), before any GPU work in this process
-    cpu = cpu_1core = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        nthreads = os.cpu_count() or 1
+    cpu = cpu_1core = core = None
+    if with_cpu:
+        nthreads = ncpu()
         sample = min(nq, args.ref_sample)
         cpu_search(ix_data, base, queries[: max(1, sample // 10)], c, nthreads)
         t, cpu_ids, cpu_dis = cpu_search(ix_data, base, queries[:sample], c, nthreads, results=True)
@@ -349,6 +502,7 @@ def run_gpu(args, c, rank, world, local_rank):
         t1 = cpu_search(ix_data, base, queries[:s1], c, 1)
         cpu_1core = {"value": s1 / t1, "unit": "queries/s", "cores": 1, "kind": "port",
                      "sample": f"{s1} queries of this workload, one thread ({t1:.2f}s)"}
+        core = core_cpu_baseline(ix_data, queries, c)
 
     gi = GpuIndex(ix_data, device=local_rank, base=base)
     stream = torch.cuda.Stream(device=dev)
@@ -363,7 +517,6 @@ def run_gpu(args, c, rank, world, local_rank):
         gi.search_device(d_q.data_ptr(), nq, k, w, d_ids.data_ptr(), d_dis.data_ptr(), kl=kl,
                          rerank=c["rerank"], stream_ptr=sp, profile=profile)
 
-    # algorithmic scan bytes: sum over queries of the probed lists' codes
     coaidx, _ = gi.coarse_assign(queries, w)
     sizes = ix_data.list_sizes().astype(np.int64)
     scan_bytes = int(sizes[coaidx].sum()) * m
@@ -383,7 +536,7 @@ def run_gpu(args, c, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     barrier()
-    step_ms, scan_ms, coarse_ms, scank_ms, fin_ms = [], [], [], [], []
+    step_ms, coarse_ms, scank_ms, fin_ms = [], [], [], []
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     for i in range(args.steps):
@@ -397,7 +550,6 @@ def run_gpu(args, c, rank, world, local_rank):
         step_ms.append(ev0.elapsed_time(ev1))
         cm, sk, fm = gi.last_stages_ms()
         coarse_ms.append(cm)
-        scan_ms.append(sk + fm)
         scank_ms.append(sk)
         fin_ms.append(fm)
     barrier()
@@ -421,44 +573,44 @@ def run_gpu(args, c, rank, world, local_rank):
     e2e_s = max_over_ranks(e2e_s, dist, dev)
     e2e = whole_job_rate(nq, args.steps, world, e2e_s)
 
-    # quality (outside every timed region)
     quality = {}
     if cpu is not None:
         quality["parity_vs_oracle"] = parity_report(h_ids[:len(cpu_ids)], h_dis[:len(cpu_ids)], cpu_ids, cpu_dis)
-        quality["cpu_baseline_1core"] = cpu_1core
     if rank == 0 and not args.no_recall:
         gt = ground_truth(base, queries, k, key, dev)
         quality.update(recall_report(h_ids, gt, k))
 
     peak, peak_kind = measured_peak_hbm()
-    # the scan kernel alone (CUDA events on the engine's stream around its launch)
     mean_scan_s = statistics.mean(scank_ms) / 1000.0
     achieved = scan_bytes / mean_scan_s / 1e9
-    traffic = profiled_traffic(args.config)
-    if rank == 0:
-        line = {
-            "metric": "QPS", "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(c), "queries_per_step": nq, "parallelism": f"replica x{world}",
-                       "l2": "flushed between steps (256 MB write)", **quality,
-                       "stage_ms": {"coarse": statistics.mean(coarse_ms), "scan": statistics.mean(scan_ms),
-                                    "scan_kernel": statistics.mean(scank_ms), "finalize": statistics.mean(fin_ms)}},
-            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(queries.nbytes),
-                    "d2h_bytes_per_step": int(nq * k * 8)},
-            "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "bytes_per_launch": scan_bytes, "bytes_unique_per_launch": unique_bytes,
-                         "traffic": traffic},
-            "cpu_baseline": cpu,
-            # norm_d, coarse_dist, coarse_select, ivf_scan_persistent, finalize per search
-            "gpu_launches": 5 * args.steps,
-            "clocks": clk,
-        }
-        print(json.dumps(line), flush=True)
     gi.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    return {
+        "metric": "QPS", "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(c), "queries_per_step": nq, "parallelism": f"replica x{world}",
+                   "l2": "flushed between steps (256 MB write)"},
+        "quality": quality,
+        "stage_ms": {"coarse": statistics.mean(coarse_ms), "scan_kernel": statistics.mean(scank_ms),
+                     "finalize": statistics.mean(fin_ms)},
+        "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(queries.nbytes),
+                "d2h_bytes_per_step": int(nq * k * 8)},
+        "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "bytes_per_launch": scan_bytes, "bytes_unique_per_launch": unique_bytes,
+                     "traffic": profiled_traffic("ivf_scan_cfg2")},
+        "cpu_baseline": cpu, "cpu_baseline_1core": cpu_1core, "cpu_baseline_core_cpu": core,
+        # norm_d, coarse_dist, coarse_select, ivf_scan_persistent, finalize per search
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk,
+    }
+
+
+# ---------------------------------------------------------------------------
+# the large workloads (GPU-built indexes, both forms as CUDA-graph replays)
+# ---------------------------------------------------------------------------
+
+FORMS = (("plain", dict(mixed_coarse=False, mixed_scan=False)), ("mixed", dict(mixed_coarse=True, mixed_scan=True)))
 
 
 def adc_error_fp64(ix, queries, res, off, kq, nsample):
@@ -493,39 +645,19 @@ def adc_error_fp64(ix, queries, res, off, kq, nsample):
     return {"max_rel": float(rel.max()), "mean_rel": float(rel.mean()), "pairs": int(rel.size)}
 
 
-def run_large(args, c, name, local_rank):
-    """Larger workloads: data and index built on the GPU; the plain FP32 form and
-    the precision form (tensor-core coarse stage) timed as CUDA-graph replays."""
+def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
+    """Both forms of a large workload timed as CUDA-graph replays, with stage split, recall against
+    an exact ground truth, FP64 distance error, oracle parity on a sample of queries and, for the
+    headline, e2e through the host C ABI and the CPU baseline."""
     import torch
 
     from mestrado_gb300.engine import GpuIndex
-    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu, exact_topk
-    from mestrado_gb300.synth import Mixture
+    from mestrado_gb300.gpu_build import exact_topk_streaming
 
-    dev = torch.device("cuda", local_rank)
-    torch.cuda.set_device(dev)
-    t0 = time.time()
-    gm = GpuMixture(Mixture(d=c["d"], ncomp=c["ncomp"], seed=c["seed"], zipf=c["zipf"]))
-    base = gm.generate(c["nbase"], stream_id=1)
-    train = gm.generate(c["ntrain"], stream_id=2)
-    queries = gm.generate(c["nq"], stream_id=3)
-    torch.cuda.synchronize()
-    t_gen = time.time() - t0
-    t0 = time.time()
-    ix = build_index_gpu(base, train, c["C"], c["m"], niter=c["train_iters"], seed=c["seed"])
-    t_build = time.time() - t0
-    del train
-    sizes = ix.list_sizes()
-    log(f"{name}: generated in {t_gen:.1f}s, index built in {t_build:.1f}s; lists {sizes.min()}..{sizes.max()}")
+    gm, ix, queries, t_build = large_inputs(name, c, dev, rank, dist)
     gi = GpuIndex(ix, device=local_rank)
-    nq = c["nq"]
-    rng = np.random.default_rng(c["seed"] + 17)
-    if c["uneven"]:
-        wq = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(c["w"] + 1), nq))), 1, c["w"]).astype(np.int32)
-        kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
-    else:
-        wq = np.full(nq, c["w"], np.int32)
-        kq = np.full(nq, c["k"], np.int32)
+    nq, m = c["nq"], c["m"]
+    wq, kq = batch_shape(c, nq)
     off = np.concatenate([[0], np.cumsum(kq)]).astype(np.int64)
     max_w, max_k = int(wq.max()), int(kq.max())
     d_w = torch.from_numpy(wq).to(dev)
@@ -536,22 +668,28 @@ def run_large(args, c, name, local_rank):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
-    # candidate bytes of the ADC scan: sum over queries of their probed lists' codes
-    coa_idx, _ = gi.coarse_assign(queries.cpu().numpy(), max_w)
-    scan_bytes = int(sum(sizes[coa_idx[i, :wq[i]]].sum() for i in range(nq))) * c["m"]
-    probed = np.unique(np.concatenate([coa_idx[i, :wq[i]] for i in range(nq)]))
-    unique_bytes = int(sizes[probed[probed >= 0]].astype(np.int64).sum()) * c["m"]
+    q_host = queries.cpu().numpy()
+    # algorithmic bytes of the ADC scan: sum over queries of their probed lists' codes
+    sizes = ix.list_sizes().astype(np.int64)
+    coa_idx, _ = gi.coarse_assign(q_host, max_w)
+    probed = np.where(np.arange(max_w)[None, :] < wq[:, None], coa_idx, -1)
+    scan_bytes = int(np.where(probed >= 0, sizes[np.maximum(probed, 0)], 0).sum()) * m
+    uniq = np.unique(probed[probed >= 0])
+    unique_bytes = int(sizes[uniq].sum()) * m
     sample = 0 if args.no_recall else min(nq, c["recall_q"])
-    gt = exact_topk(base, queries[:sample], max_k, batch=16 if c["nbase"] > 20_000_000 else 64) if sample else None
-    del base
-    torch.cuda.empty_cache()
+    gt = exact_topk_streaming(gm, c["nbase"], queries[:sample], max_k) if sample else None
 
-    q_host = queries[:sample].cpu().numpy() if sample else None
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
     forms = {}
-    for form, mixed in (("plain", False), ("mixed", True)):
+    for form, fl in FORMS:
         graph = gi.capture_graph(queries.data_ptr(), nq, max_k, max_w, d_ids.data_ptr(), d_dis.data_ptr(),
-                                 mixed_coarse=mixed, mixed_scan=mixed, d_w_ptr=d_w.data_ptr(),
-                                 d_k_ptr=d_k.data_ptr(), d_off_ptr=d_off.data_ptr(), stream_ptr=sp)
+                                 d_w_ptr=d_w.data_ptr(), d_k_ptr=d_k.data_ptr(), d_off_ptr=d_off.data_ptr(),
+                                 stream_ptr=sp, **fl)
+        kernels = graph.kernel_count()
         for i in range(args.warmup):
             graph.launch(sp)
         stream.synchronize()
@@ -559,6 +697,7 @@ def run_large(args, c, name, local_rank):
         ev1 = torch.cuda.Event(enable_timing=True)
         clocks = ClockSampler(local_rank)
         clocks.start()
+        barrier()
         total = 0.0
         for i in range(args.steps):
             with torch.cuda.stream(stream):
@@ -569,62 +708,243 @@ def run_large(args, c, name, local_rank):
                 ev1.record(stream)
             ev1.synchronize()
             total += ev0.elapsed_time(ev1)
+        barrier()
         clk = clocks.stop()
         graph.close()
+        total = max_over_ranks(total, dist, dev)
         ids = d_ids.cpu().numpy()
-        # stage split from one profiled (non-graph) run
-        gi.lib.gbivf_search_batched_device(gi.h, C_ptr(queries), nq, C_ptr(d_w), C_ptr(d_k), C_ptr(d_off),
-                                           max_w, max_k, 0x100 | (0x14 if mixed else 0), C_ptr(d_ids),
-                                           C_ptr(d_dis), sp_ptr(sp))
-        stages = stage_split(gi)
-        rec = [len(set(ids[off[i]:off[i] + kq[i]].tolist()) & set(gt[i, :kq[i]].tolist())) / kq[i]
-               for i in range(sample)] or [float("nan")]
         dis = d_dis.cpu().numpy()
-        forms[form] = dict(qps=nq * args.steps / (total / 1000.0), ms_per_step=total / args.steps,
-                           stages=stages, recall=float(np.mean(rec)), clocks=clk, ids=ids, dis=dis,
-                           err=adc_error_fp64(ix, q_host, (ids, dis), off, kq, min(sample, 100)))
-    pi, mi = forms["plain"]["ids"], forms["mixed"]["ids"]
-    same_rows = float(np.mean([np.array_equal(pi[off[i]:off[i + 1]], mi[off[i]:off[i + 1]]) for i in range(nq)]))
-    overlap = float(np.mean([len(set(pi[off[i]:off[i + 1]].tolist()) & set(mi[off[i]:off[i + 1]].tolist())) / kq[i]
-                             for i in range(nq)]))
-    # every distance the mixed form returns for an id the plain form also returns must be identical
-    pd_, md_ = forms["plain"]["dis"], forms["mixed"]["dis"]
-    mismatch = 0
-    for i in range(nq):
-        a = dict(zip(pi[off[i]:off[i + 1]].tolist(), pd_[off[i]:off[i + 1]].view(np.uint32).tolist()))
-        for idv, dv in zip(mi[off[i]:off[i + 1]].tolist(), md_[off[i]:off[i + 1]].view(np.uint32).tolist()):
-            mismatch += int(idv in a and a[idv] != dv)
-    same = same_rows == 1.0
+        # stage split: the mean of three profiled (non-graph) searches
+        st = []
+        for _ in range(3):
+            flush.fill_(1)
+            gi.search_batched_device(queries.data_ptr(), nq, d_w.data_ptr(), d_k.data_ptr(), d_off.data_ptr(),
+                                     max_w, max_k, d_ids.data_ptr(), d_dis.data_ptr(), stream_ptr=sp, profile=True,
+                                     **fl)
+            st.append(stage_split(gi))
+        stages = {k_: statistics.mean(s[k_] for s in st) for k_ in st[0]}
+        rec = packed_recall(ids, off, kq, gt, sample) if sample else {}
+        forms[form] = dict(qps=whole_job_rate(nq, args.steps, world, total / 1000.0), ms_per_step=total / args.steps,
+                           stages=stages, gpu_launches_per_step=kernels, clocks=clk, ids=ids, dis=dis, **rec,
+                           adc_distance_error_vs_fp64=adc_error_fp64(ix, q_host, (ids, dis), off, kq,
+                                                                     min(sample or 100, 100)))
+    pl, mx = forms["plain"], forms["mixed"]
+    plain_vs_mixed = packed_parity(mx["ids"], mx["dis"], pl["ids"], pl["dis"], off, nq)
+
+    # the plain form (the drop-in) against the oracle on a sample of queries, over the same index
+    par = None
+    if rank == 0 and args.parity_sample > 0:
+        ns = min(nq, args.parity_sample)
+        t_or, (o_ids, o_dis, o_off) = cpu_batched(ix, q_host[:ns], wq[:ns], kq[:ns], ncpu())
+        par = packed_parity(pl["ids"][:off[ns]], pl["dis"][:off[ns]], o_ids, o_dis, o_off, ns)
+        par["ties"] = "both keyed by (distance, position in the probe order)"
+        par["oracle_seconds"] = t_or
+        par["largest_k_in_sample"] = int(kq[:ns].max())
+        par["largest_nprobe_in_sample"] = int(wq[:ns].max())
+
     peak, peak_kind = measured_peak_hbm()
-    mx = forms["mixed"]
     achieved = scan_bytes / (mx["stages"]["scan_kernel"] / 1000.0) / 1e9
-    wl = (f"{name}: base {c['nbase']:,} x d=128 ({c['ncomp']}-component mixture"
-          f"{', Zipf ' + str(c['zipf']) if c['zipf'] else ''}), C={c['C']:,} lists, m={c['m']}x256, "
-          f"{nq:,} queries/step, " + (f"nprobe log-uniform 1..{c['w']}, k in {{1,10,100,1000}}" if c["uneven"]
-                                        else f"w={c['w']}, k={c['k']}"))
+    rec = {
+        "workload": large_workload(name, c),
+        "forms": {f: {k_: v for k_, v in forms[f].items() if k_ not in ("ids", "dis", "clocks")} for f in forms},
+        "mixed_over_plain_qps": mx["qps"] / pl["qps"],
+        "recall@100_delta": (None if mx.get("recall@100") is None else mx["recall@100"] - pl["recall@100"]),
+        "recall_sample_queries": sample,
+        "mixed_vs_plain": plain_vs_mixed,
+        "parity_plain_vs_oracle": par,
+        "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel (mixed form)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "bytes_per_launch": scan_bytes, "bytes_unique_per_launch": unique_bytes,
+                     "traffic": profiled_traffic(f"ivf_scan_{name}")},
+        "index_build_s": t_build,
+        "clocks": mx["clocks"], "clocks_plain": pl["clocks"],
+    }
+
+    if headline:
+        # end to end through the host C ABI: pinned queries, nprobe and k in, packed ids / dis out
+        h_q = torch.from_numpy(q_host).pin_memory().numpy()
+        h_w = torch.from_numpy(wq).pin_memory().numpy()
+        h_k = torch.from_numpy(kq).pin_memory().numpy()
+        h_ids = torch.empty(int(off[-1]), dtype=torch.int32).pin_memory().numpy()
+        h_dis = torch.empty(int(off[-1]), dtype=torch.float32).pin_memory().numpy()
+        mixed_fl = dict(FORMS)["mixed"]
+        for _ in range(2):
+            gi.search_batched(h_q, h_w, h_k, out=(h_ids, h_dis), **mixed_fl)
+        e2e_s = 0.0
+        for i in range(args.steps):
+            flush.fill_((i + 7) & 0xff)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            gi.search_batched(h_q, h_w, h_k, out=(h_ids, h_dis), **mixed_fl)
+            e2e_s += time.perf_counter() - t
+        e2e_s = max_over_ranks(e2e_s, dist, dev)
+        same = bool(np.array_equal(h_ids, mx["ids"]))
+        rec["e2e"] = {"value": whole_job_rate(nq, args.steps, world, e2e_s), "unit": "queries/s",
+                      "h2d_bytes_per_step": int(h_q.nbytes + h_w.nbytes + h_k.nbytes),
+                      "d2h_bytes_per_step": int(h_ids.nbytes + h_dis.nbytes),
+                      "api": "gbivf_search_batched (host buffers, mixed form)", "ids_equal_device_run": same}
+        # the oracle on all host cores, on a sample of the same queries sized to ~10 s
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            t32, _ = cpu_batched(ix, q_host[:32], wq[:32], kq[:32], ncpu())
+            ns = sample_size(t32 / 32, 10.0, 64, nq)
+            t, _ = cpu_batched(ix, q_host[:ns], wq[:ns], kq[:ns], ncpu())
+            rec["cpu_baseline"] = {"value": ns / t, "unit": "queries/s", "cores": ncpu(), "kind": "port",
+                                   "sample": f"the first {ns} of the {nq} queries (their own nprobe and k), "
+                                             f"OpenMP over queries ({t:.2f}s)"}
+    gi.close()
+    return rec
+
+
+def run_headline(args, rank, world, local_rank):
+    import torch
+
+    name, c = HEADLINE, LARGE[HEADLINE]
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    rec = large_record(args, name, c, dev, rank, world, dist, local_rank, headline=True)
+    sub = {}
+    if world == 1 and not args.no_sub:
+        for sub_name, fn in (("drop_in_cfg2", lambda: drop_in_record(args, CONFIGS["cfg2"], rank, world, None, dev,
+                                                                     local_rank)),
+                             ("cfg3", lambda: large_record(args, "cfg3", LARGE["cfg3"], dev, rank, world, None,
+                                                           local_rank, headline=False))):
+            try:
+                sub[sub_name] = fn()
+            except Exception as e:  # a failed sub-record must not lose the headline
+                sub[sub_name] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
+    if rank == 0:
+        mx, pl = rec["forms"]["mixed"], rec["forms"]["plain"]
+        line = {
+            "metric": METRIC, "value": mx["qps"], "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "mixed: bf16 tensor-core coarse + f32 re-check, f16 tables with f32 accumulation and f32 "
+                     "re-score (plain form: f32)",
+            "data": "synthetic",
+            "config": large_config(name, c),
+            "forms": {"mixed_qps": mx["qps"], "plain_qps": pl["qps"], "mixed_over_plain": rec["mixed_over_plain_qps"],
+                      "recall@100_mixed": mx.get("recall@100"), "recall@100_plain": pl.get("recall@100"),
+                      "recall@100_delta": rec["recall@100_delta"], "adc_scan_gbs": rec["roofline"]["achieved"],
+                      "detail": rec["forms"], "mixed_vs_plain": rec["mixed_vs_plain"]},
+            "parity": rec["parity_plain_vs_oracle"],
+            "e2e": rec.get("e2e"),
+            "roofline": rec["roofline"],
+            "cpu_baseline": rec.get("cpu_baseline"),
+            "gpu_launches": mx["gpu_launches_per_step"] * args.steps,
+            "clocks": rec["clocks"],
+            "index_build_s": rec["index_build_s"],
+            "sub": sub,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference_headline(args, rank, world):
+    """The oracle alone on the headline workload: each step searches a bounded sample of the batch
+    (rotating through it), every host thread."""
+    if rank != 0:
+        return
+    import torch
+
+    name, c = HEADLINE, LARGE[HEADLINE]
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _, ix, queries, _ = large_inputs(name, c, dev)
+    q_host = queries.cpu().numpy()
+    del queries
+    torch.cuda.empty_cache()
+    nq = c["nq"]
+    wq, kq = batch_shape(c, nq)
+    t32, _ = cpu_batched(ix, q_host[:32], wq[:32], kq[:32], ncpu())
+    # about 1.5 s of CPU work per step
+    ns = sample_size(t32 / 32, 1.5, 32, nq)
+
+    def step(i):
+        s = (i * ns) % nq
+        sl = slice(s, min(nq, s + ns))
+        return cpu_batched(ix, q_host[sl], wq[sl], kq[sl], ncpu())[0], sl.stop - sl.start
+
+    for i in range(args.warmup):
+        step(i)
+    ts = [step(args.warmup + i) for i in range(args.steps)]
+    total = sum(t for t, _ in ts)
+    done = sum(n for _, n in ts)
+    qps = done / total
     line = {
-        "metric": "QPS", "value": mx["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16 tensor-core coarse + fp32 re-check; fp16 tables, fp32 re-score",
-        "data": "synthetic",
-        "config": {"workload": wl, "form": "mixed: tensor-core coarse stage and fp16-table scan with the "
-                   f"{4}k best re-scored in fp32; CUDA-graph replay",
-                   "plain_qps": forms["plain"]["qps"], "speedup_vs_plain": mx["qps"] / forms["plain"]["qps"],
-                   "identical_ids_plain_vs_mixed": same, "identical_rows_fraction": same_rows,
-                   "id_overlap_with_plain": overlap, "distance_mismatches_on_shared_ids": mismatch,
-                   f"recall_sample_queries": sample,
-                   "recall_mixed": mx["recall"], "recall_plain": forms["plain"]["recall"],
-                   "adc_distance_error_vs_fp64": {"plain": forms["plain"]["err"], "mixed": mx["err"]},
-                   "stage_ms_mixed": mx["stages"], "stage_ms_plain": forms["plain"]["stages"],
-                   "index_build_s": t_build, "generate_s": t_gen, "l2": "flushed between steps (256 MB write)"},
-        "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": scan_bytes,
-                     "bytes_unique_per_launch": unique_bytes, "traffic": None},
-        "cpu_baseline": None,
-        "clocks": mx["clocks"],
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": large_config(name, c),
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": ncpu(), "kind": "port",
+                         "sample": f"{ns} of the {nq} queries per step (consecutive slices), OpenMP over queries"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
-    gi.close()
+
+
+def run_reference(args, c, rank, world):
+    """The oracle alone on a drop-in workload (cfg1 / cfg2)."""
+    if rank != 0:
+        return
+    ix, base, queries, _ = make_inputs(c, 0)
+    nthreads = ncpu()
+    sample = min(len(queries), args.ref_sample)
+    qs = queries[:sample]
+    for _ in range(args.warmup):
+        cpu_search(ix, base, qs[: max(1, sample // 10)], c, nthreads)
+    ts = [cpu_search(ix, base, qs, c, nthreads) for _ in range(args.steps)]
+    total = sum(ts)
+    qps = sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": "QPS", "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": workload_name(c), "queries_per_step": c["nq"],
+                                        "parallelism": f"replica x{world}",
+                                        "l2": "flushed between steps (256 MB write)"},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{sample} of the {c['nq']} queries per step"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_drop_in(args, c, rank, world, local_rank):
+    import torch
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    line = drop_in_record(args, c, rank, world, dist, dev, local_rank,
+                          with_cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_large_line(args, name, local_rank):
+    import torch
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    rec = large_record(args, name, LARGE[name], dev, 0, 1, None, local_rank, headline=False)
+    mx = rec["forms"]["mixed"]
+    line = {"metric": METRIC, "value": mx["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mx["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "data": "synthetic", "config": large_config(name, LARGE[name]), **rec}
+    print(json.dumps(line), flush=True)
 
 
 def run_stream(args, c, name, local_rank):
@@ -789,28 +1109,19 @@ def check_rc(rc, gi):
         raise RuntimeError(f"gbivf error {rc}: {gi.lib.gbivf_last_error().decode()}")
 
 
-def C_ptr(t):
-    import ctypes
-
-    return ctypes.c_void_p(t.data_ptr())
-
-
-def sp_ptr(s):
-    import ctypes
-
-    return ctypes.c_void_p(s)
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbivf", choices=["gbivf", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS) + sorted(LARGE))
-    ap.add_argument("--ref-sample", type=int, default=10_000, help="queries per CPU step")
+    ap.add_argument("--config", default=HEADLINE, choices=sorted(CONFIGS) + sorted(LARGE))
+    ap.add_argument("--ref-sample", type=int, default=10_000, help="drop-in workloads: queries per CPU step")
+    ap.add_argument("--parity-sample", type=int, default=128,
+                    help="large workloads: queries checked against the oracle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="headline: skip the drop-in and 10M sub-records")
     ap.add_argument("--stage", default="search", choices=["search", "coarse"],
                     help="large configurations: time the whole search, or the coarse stage alone")
     ap.add_argument("--nbase", type=int, default=None,
@@ -824,24 +1135,31 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.config in LARGE and args.nbase:
         LARGE[args.config] = dict(LARGE[args.config], nbase=args.nbase)
+    if args.config == HEADLINE and args.stage == "search":
+        if args.impl == "reference":
+            run_reference_headline(args, rank, world)
+        else:
+            run_headline(args, rank, world, local_rank)
+        return
     if args.config in LARGE:
         if args.impl == "reference" or world > 1:
             if rank == 0:
-                print(json.dumps({"impl": args.impl, "unavailable": "the large configurations run the GPU engine "
-                                  "alone, on one GPU (the CPU oracle over 10M-100M vectors takes hours)"}))
+                print(json.dumps({"impl": args.impl, "unavailable": "this workload runs the GPU engine alone, on "
+                                  "one GPU; the headline workload (the default) has the reference arm"}))
             return
+        c = LARGE[args.config]
         if args.stage == "coarse":
-            run_coarse(args, LARGE[args.config], args.config, local_rank)
-        elif LARGE[args.config].get("stream"):
-            run_stream(args, LARGE[args.config], args.config, local_rank)
+            run_coarse(args, c, args.config, local_rank)
+        elif c.get("stream"):
+            run_stream(args, c, args.config, local_rank)
         else:
-            run_large(args, LARGE[args.config], args.config, local_rank)
+            run_large_line(args, args.config, local_rank)
         return
     c = CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, c, rank, world)
     else:
-        run_gpu(args, c, rank, world, local_rank)
+        run_drop_in(args, c, rank, world, local_rank)
 
 
 if __name__ == "__main__":

@@ -64,6 +64,15 @@ extern "C" {
                                      cheap against the 4096-entry exact table). Falls back to the exact
                                      form where the precision form does not apply. Not combined with
                                      GBIVF_MIXED_SCAN */
+#define GBIVF_LIST_SCAN 0x80u   /* scan list by list: the batch's (query, probe) pairs grouped by list,
+                                   one work item per list and group of 4 (exact form) or 8 (precision
+                                   form) queries, their tables interleaved so that one 16-byte shared
+                                   load serves the group; each query's top-k through a threshold from
+                                   a scan of its nearest probes. Same results as the per-query scan.
+                                   Not with GBIVF_TABLE_DIRECT or GBIVF_QUERY_SCAN */
+#define GBIVF_QUERY_SCAN 0x200u /* scan query by query (one CTA per query at a time). Without either
+                                   flag the engine picks: the list-centric scan for batches of at
+                                   least 1024 queries where it applies */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -169,6 +178,9 @@ int gbivf_graph_capture(gbivf_index *ix, const float *d_queries, int nq, int k, 
                         const int32_t *d_k, const int64_t *d_out_off, void *stream, gbivf_graph **out);
 int gbivf_graph_launch(gbivf_graph *g, void *stream);
 int gbivf_graph_destroy(gbivf_graph *g);
+/* Kernel launches one replay of the graph makes (its kernel nodes; memsets
+ * and copies are not counted). No counterpart in the reference. */
+int gbivf_graph_kernel_count(const gbivf_graph *g, int *kernels);
 
 /* Autotuner: times the scan kernels that can serve this index and search
  * shape (persistent register-codebook kernel with 512 or 1024 threads, or the
@@ -197,6 +209,16 @@ int gbivf_last_stage_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms);
  * of gbivf_last_stage_ms. */
 int gbivf_last_stages_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms, float *finalize_ms);
 
+/* The parts of the last GBIVF_PROFILE search's scan stage when it ran list by
+ * list (GBIVF_LIST_SCAN), in ms: [0] planning, [1] the first pass over each
+ * query's nearest probes, [2] grouping the pairs by list, [3] the list-centric
+ * scan kernel, [4] selection, [5] the pass over overflowed queries, [6]
+ * finalize; and its counters: [0] (query, probe) pairs scanned list by list,
+ * [1] work items, [2] queries that overflowed their buffer, [3] 1 if the scan
+ * ran list by list. Either array may be NULL. Waits for the search. No
+ * counterpart in the reference. */
+int gbivf_last_scan_parts(gbivf_index *ix, float *parts_ms, int64_t *counters);
+
 /* The coarse stage alone: knn_full(2, nq, C, d, w, coa, queries, ...)
  * (sequential/ivf_pq/ivf_search.cpp:37-38): the w nearest lists per query,
  * ascending. coaidx, coadis: nq x w host arrays. */
@@ -215,10 +237,12 @@ int gbivf_coarse_assign(gbivf_index *ix, const float *queries, int nq, int w, in
  * allocates nothing: its scratch is one file-scope device array of
  * GBIVF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * exit, so nq * (8 + 4 * coarsek) plus alignment must fit in it (larger
- * calls return GBIVF_ERR_UNSUPPORTED; split the batch). The first call on a
- * device looks up the array's address (cudaGetSymbolAddress), so make it
- * before any stream capture. Calls that overlap on the GPU share the array
- * and race. No counterpart in the reference. */
+ * calls return GBIVF_ERR_UNSUPPORTED; split the batch: 4,088 queries at
+ * coarsek = 1024). The first call on a device, and the first after the
+ * device's context was replaced (cudaDeviceReset), looks up the array's
+ * address (cudaGetSymbolAddress), so make it before any stream capture.
+ * Calls that overlap on the GPU share the array and race. No counterpart in
+ * the reference. */
 int gbivf_coarse_assign_noalloc(gbivf_index *ix, const float *d_queries, int nq, int w,
                                 int32_t *d_coaidx, float *d_coadis, void *stream);
 

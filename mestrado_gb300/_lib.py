@@ -18,6 +18,8 @@ GBIVF_COARSE_FULL = 0x8
 GBIVF_MIXED_SCAN = 0x10
 GBIVF_RERANK_REFINE = 0x20
 GBIVF_MIXED_SCAN_AUTO = 0x40
+GBIVF_LIST_SCAN = 0x80
+GBIVF_QUERY_SCAN = 0x200
 GBIVF_PROFILE = 0x100
 
 _lib = None
@@ -29,10 +31,10 @@ EXPORTS = [
     "gbivf_ivfpq_search_device", "gbivf_coarse_assign", "gbivf_core_gpu", "gbivf_pq_create",
     "gbivf_pq_search", "gbivf_last_stage_ms", "gbivf_coarse_assign_noalloc", "gbivf_coarse_assign_flags",
     "gbivf_search_batched", "gbivf_search_batched_device", "gbivf_graph_capture", "gbivf_graph_launch",
-    "gbivf_graph_destroy", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
+    "gbivf_graph_destroy", "gbivf_graph_kernel_count", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
     "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats", "gbivf_coarse_assign_device",
     "gbivf_index_set_refine", "gbivf_index_set_refine_device", "gbivf_pq_error", "gbivf_index_create_device",
-    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_selftest_wait_timeout", "gbivf_index_scan_form",
+    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_last_scan_parts", "gbivf_selftest_wait_timeout", "gbivf_index_scan_form",
 ]
 
 
@@ -69,6 +71,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_pq_search.argtypes = [vp, vp, i32, i32, vp, vp]
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     lib.gbivf_last_stages_ms.argtypes = [vp, vp, vp, vp]
+    lib.gbivf_last_scan_parts.argtypes = [vp, vp, vp]
     lib.gbivf_index_scan_form.argtypes = [vp, vp, vp]
     lib.gbivf_selftest_wait_timeout.argtypes = [C.c_int, vp, vp, vp]
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]
@@ -82,6 +85,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_assign_flags.argtypes = [vp, i64, i32, vp, i32, vp, u32, vp]
     lib.gbivf_search_batched.argtypes = [vp, vp, i32, vp, vp, u32, vp, vp]
     lib.gbivf_search_batched_device.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, u32, vp, vp, vp]
+    lib.gbivf_graph_kernel_count.argtypes = [vp, vp]
     lib.gbivf_graph_capture.argtypes = [vp, vp, i32, i32, i32, i32, u32, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
     lib.gbivf_graph_launch.argtypes = [vp, vp]
     lib.gbivf_graph_destroy.argtypes = [vp]

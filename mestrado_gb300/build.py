@@ -24,7 +24,7 @@ LIB = os.path.join(LIBDIR, "libgbivf.so")
 SHIMS = {"libgbivf_refcompat_seq.so": "refcompat_seq.cpp", "libgbivf_refcompat_par2.so": "refcompat_par2.cpp"}
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["kernels.cu", "scan_persistent.cu", "coarse_mma.cu", "coarse_filter.cu", "coarse_gemm.cu", "build_gpu.cu", "api.cu"]
+SOURCES = ["kernels.cu", "scan_persistent.cu", "scan_lists.cu", "coarse_mma.cu", "coarse_filter.cu", "coarse_gemm.cu", "build_gpu.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",

@@ -15,6 +15,8 @@
 #include <limits>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/gbivf.h"
 #include "exact_round.cuh"
 #include "kernels.cuh"
@@ -131,6 +133,13 @@ struct gbivf_index {
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
     // hand-off lists of the precision form and the refinement re-rank
     DBuf w_clist;
+    // list-centric scan (scan_lists.cu): one workspace block, its layout, stage events
+    DBuf lc_ws;
+    ListScanWork lcw;
+    cudaEvent_t lc_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool last_list_scan = false;      // the last profiled search scanned list by list
+    bool list_default = true;         // without GBIVF_LIST_SCAN / GBIVF_QUERY_SCAN: list by list for large batches
+    int lc_ecap = 0;                  // per-query emission capacity of the list-centric scan (0: the default)
     // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_valid = false;
@@ -157,11 +166,13 @@ void free_index(gbivf_index* ix) {
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
                     &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->w_clist,
-                    &ix->pq2, &ix->codes2})
+                    &ix->pq2, &ix->codes2, &ix->lc_ws})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
     for (auto& e : ix->ev)
+        if (e) cudaEventDestroy(e), e = nullptr;
+    for (auto& e : ix->lc_ev)
         if (e) cudaEventDestroy(e), e = nullptr;
 }
 
@@ -251,7 +262,14 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     }
     if (cudaDeviceGetAttribute(&ix->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) ix->num_sms = 1;
     if (const char* v = getenv("GBIVF_SCAN_THREADS")) ix->scan_threads = atoi(v) == 1024 ? 1024 : 512;
-    if (const char* v = getenv("GBIVF_SCAN_KERNEL")) ix->use_persistent = strcmp(v, "general") != 0;
+    // a smaller emission buffer than the default sends more queries through the overflow pass
+    if (const char* v = getenv("GBIVF_LIST_SCAN_CAP")) ix->lc_ecap = std::max(0, atoi(v));
+    // rows of the first pass per selected candidate (its threshold tightens as it grows)
+    if (const char* v = getenv("GBIVF_LIST_SCAN_BETA")) ix->lcw.beta = std::max(1, atoi(v));
+    if (const char* v = getenv("GBIVF_SCAN_KERNEL")) {
+        ix->use_persistent = strcmp(v, "general") != 0;
+        ix->list_default = strcmp(v, "lists") == 0;
+    }
 
     DevIndex& dx = ix->dx;
     dx.d = d;
@@ -325,8 +343,54 @@ int coarse_batch(int nq, int C) {
     return (int)std::max<int64_t>(1, bq);
 }
 
-// the persistent register-codebook kernel where it applies, else the general one
-int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nullptr) {
+// Workspace of the list-centric scan for this search shape, carved from one device block.
+int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
+    const int64_t nq = a.nq, C = ix->dx.C, P = nq * a.w;
+    ListScanWork& w = ix->lcw;
+    w.ecap = ix->lc_ecap > 0 ? std::min(ix->lc_ecap, list_scan_ecap(a)) : list_scan_ecap(a);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t r = off;
+        off += (bytes + 255) / 256 * 256;
+        return r;
+    };
+    const size_t o_w0 = take(4 * nq), o_pcnt = take(4 * C), o_pbeg = take(4 * (C + 1)), o_fill = take(4 * C),
+                 o_gbeg = take(4 * (C + 1)), o_pairs = take(16 * P), o_groups = take(16 * P), o_cnt = take(4 * 8),
+                 o_keys = take(8 * nq * a.cand_stride), o_cntA = take(4 * nq), o_tau = take(8 * nq),
+                 o_ebuf = take(8 * nq * (int64_t)w.ecap), o_ecnt = take(4 * nq), o_ovf = take(4 * nq);
+    CK(ix->lc_ws.ensure(off));
+    unsigned char* b = ix->lc_ws.as<unsigned char>();
+    w.w0 = reinterpret_cast<int*>(b + o_w0);
+    w.pcnt = reinterpret_cast<int*>(b + o_pcnt);
+    w.pbeg = reinterpret_cast<int*>(b + o_pbeg);
+    w.fill = reinterpret_cast<int*>(b + o_fill);
+    w.gbeg = reinterpret_cast<int*>(b + o_gbeg);
+    w.pairs = reinterpret_cast<int4*>(b + o_pairs);
+    w.groups = reinterpret_cast<int4*>(b + o_groups);
+    w.counters = reinterpret_cast<int*>(b + o_cnt);  // [0..2] groups, work counter, overflows; [3], [4] queues
+    w.queue_a = w.counters + 3;
+    w.queue_b = w.counters + 4;
+    w.keysA = reinterpret_cast<unsigned long long*>(b + o_keys);
+    w.cntA = reinterpret_cast<int*>(b + o_cntA);
+    w.tau = reinterpret_cast<unsigned long long*>(b + o_tau);
+    w.ebuf = reinterpret_cast<unsigned long long*>(b + o_ebuf);
+    w.ecnt = reinterpret_cast<int*>(b + o_ecnt);
+    w.ovf = reinterpret_cast<int32_t*>(b + o_ovf);
+    CK(ix->w_flags.ensure(4 * sizeof(int)));
+    w.err = ix->w_flags.as<int>();
+    return GBIVF_OK;
+}
+
+// whether this search scans list by list (GBIVF_LIST_SCAN, or the engine's choice for large batches)
+bool use_list_scan(const gbivf_index* ix, const ScanArgs& a, unsigned gflags) {
+    if (gflags & GBIVF_QUERY_SCAN) return false;
+    const bool want = (gflags & GBIVF_LIST_SCAN) || (ix->list_default && a.nq >= 1024);
+    return want && list_scan_supported(ix->dx, a);
+}
+
+// the list-centric pipeline, the persistent register-codebook kernel where it applies, else the
+// general one
+int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nullptr, unsigned gflags = 0) {
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
     const bool mixed = a.flags & SCAN_MIXED;
@@ -340,7 +404,12 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
     const bool refine = a.flags & SCAN_REFINE;
     if (refine && !scan_persistent_supported(ix->dx, a))
         return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_RERANK_REFINE needs d = 128, ks = 256, m in {4, 8, 16}");
-    if (mixed || refine || (ix->use_persistent && scan_persistent_supported(ix->dx, a))) {
+    const bool lists = use_list_scan(ix, a, gflags);
+    if (!lists && (gflags & GBIVF_LIST_SCAN))
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_LIST_SCAN needs d = 128, ks = 256, m in {4, 8, 16}, k (or kl) "
+                                           "<= 1024 and the expansion tables");
+    ix->last_list_scan = lists;
+    if (lists || mixed || refine || (ix->use_persistent && scan_persistent_supported(ix->dx, a))) {
         const int stride = scan_persistent_stride(a);
         CK(ix->w_ckey.ensure(sizeof(unsigned long long) * (size_t)a.nq * stride));
         CK(ix->w_cid.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
@@ -353,7 +422,25 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
             CK(ix->w_clist.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
             a.cand_list = ix->w_clist.as<int32_t>();
         }
-        CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st, mid));
+        if (lists) {
+            if (!(a.flags & (SCAN_MIXED | SCAN_REFINE))) {  // the select kernel writes lists only for those
+                a.cand_list = nullptr;
+            } else if (!a.cand_list) {
+                return fail(GBIVF_ERR_INVALID, "hand-off lists missing");
+            }
+            int rc = prepare_list_scan(ix, a);
+            if (rc) return rc;
+            const bool prof = mid != nullptr;
+            if (prof)
+                for (auto& e : ix->lc_ev)
+                    if (!e) CK(cudaEventCreate(&e));
+            CK(launch_list_scan(ix->dx, a, ix->lcw, ix->num_sms, st, prof ? ix->lc_ev : nullptr));
+            ix->mixed_pending = true;  // the scan's bounded waits report through the device flags
+            if (mid) CK(cudaEventRecord(mid, st));
+            CK(launch_finalize(ix->dx, a, st));
+        } else {
+            CK(launch_scan_persistent(ix->dx, a, ix->num_sms, ix->scan_threads, st, mid));
+        }
     } else {
         CK(launch_scan(ix->dx, a, st));
         if (mid) CK(cudaEventRecord(mid, st));  // one kernel: no separate finalize
@@ -368,8 +455,12 @@ int check_search(gbivf_index* ix, int nq, int k, int kl, int w, unsigned flags) 
     if (w <= 0 || w > ix->dx.C) return fail(GBIVF_ERR_INVALID, "w=%d must be in 1..coarsek=%d", w, ix->dx.C);
     if (w > MAX_W) return fail(GBIVF_ERR_UNSUPPORTED, "w=%d > %d", w, MAX_W);
     if (flags & ~(GBIVF_RERANK | GBIVF_TABLE_DIRECT | GBIVF_PROFILE | GBIVF_MIXED_COARSE | GBIVF_COARSE_FULL |
-                  GBIVF_MIXED_SCAN | GBIVF_RERANK_REFINE | GBIVF_MIXED_SCAN_AUTO))
+                  GBIVF_MIXED_SCAN | GBIVF_RERANK_REFINE | GBIVF_MIXED_SCAN_AUTO | GBIVF_LIST_SCAN | GBIVF_QUERY_SCAN))
         return fail(GBIVF_ERR_INVALID, "unknown flags 0x%x", flags);
+    if ((flags & GBIVF_LIST_SCAN) && (flags & GBIVF_QUERY_SCAN))
+        return fail(GBIVF_ERR_INVALID, "GBIVF_LIST_SCAN and GBIVF_QUERY_SCAN exclude each other");
+    if ((flags & GBIVF_LIST_SCAN) && (flags & GBIVF_TABLE_DIRECT))
+        return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_LIST_SCAN uses the expansion tables (not GBIVF_TABLE_DIRECT)");
     if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_MIXED_SCAN_AUTO))
         return fail(GBIVF_ERR_INVALID, "GBIVF_MIXED_SCAN_AUTO chooses the scan form: not with GBIVF_MIXED_SCAN");
     if ((flags & GBIVF_MIXED_SCAN) && (flags & GBIVF_TABLE_DIRECT))
@@ -588,7 +679,8 @@ int check_device_flags(gbivf_index* ix) {
     CK(cudaMemcpy(h, ix->w_flags.p, sizeof(h), cudaMemcpyDeviceToHost));
     ix->last_ncand = h[1];
     ix->last_fallbacks = h[2];
-    if (h[0]) return fail(GBIVF_ERR_TIMEOUT, "tensor-core coarse stage: a bounded wait ran out");
+    if (h[0]) return fail(GBIVF_ERR_TIMEOUT, "a bounded device-side wait ran out (tensor-core coarse stage or "
+                                             "list-centric scan)");
     return GBIVF_OK;
 }
 
@@ -628,6 +720,9 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
         CK(cudaEventRecord(ix->ev[0], st));
     }
     ix->ev_valid = false;
+    // device flags ([0] a bounded wait ran out, [1], [2] coarse-stage counters), cleared per search
+    CK(ix->w_flags.ensure(4 * sizeof(int)));
+    CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
     CK(launch_norm_d(d_q, nq, dx.d, qn, st));
     {
         int rc = coarse_stage(ix, d_q, qn, nq, w, flags, coaidx, coadis, st);
@@ -650,7 +745,7 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     a.out_off = d_off;
     if (prof) CK(cudaEventRecord(ix->ev[1], st));
     {
-        int rs = run_scan(ix, a, st, prof ? ix->ev[3] : nullptr);
+        int rs = run_scan(ix, a, st, prof ? ix->ev[3] : nullptr, flags);
         if (rs) return rs;
     }
     if (prof) {
@@ -870,6 +965,38 @@ int gbivf_last_stages_ms(gbivf_index* ix, float* coarse_ms, float* scan_ms, floa
     return GBIVF_OK;
 }
 
+int gbivf_last_scan_parts(gbivf_index* ix, float* parts_ms, int64_t* counters) {
+    if (!ix) return fail(GBIVF_ERR_INVALID, "index is NULL");
+    if (!ix->ev_valid) return fail(GBIVF_ERR_INVALID, "no search with GBIVF_PROFILE since the last one without");
+    DeviceGuard g(ix->device);
+    CK(cudaEventSynchronize(ix->ev[2]));
+    const bool lists = ix->last_list_scan;
+    if (parts_ms) {
+        for (int i = 0; i < 7; i++) parts_ms[i] = 0.0f;
+        if (lists) {
+            cudaEvent_t seq[8] = {ix->ev[1], ix->lc_ev[0], ix->lc_ev[1], ix->lc_ev[2],
+                                  ix->lc_ev[3], ix->lc_ev[4], ix->ev[3], ix->ev[2]};
+            for (int i = 0; i < 7; i++) CK(cudaEventElapsedTime(&parts_ms[i], seq[i], seq[i + 1]));
+        } else {
+            CK(cudaEventElapsedTime(&parts_ms[3], ix->ev[1], ix->ev[3]));
+            CK(cudaEventElapsedTime(&parts_ms[6], ix->ev[3], ix->ev[2]));
+        }
+    }
+    if (counters) {
+        for (int i = 0; i < 4; i++) counters[i] = 0;
+        if (lists) {
+            int h[3] = {0, 0, 0}, npairs = 0;
+            CK(cudaMemcpy(h, ix->lcw.counters, sizeof(h), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(&npairs, ix->lcw.pbeg + ix->dx.C, sizeof(int), cudaMemcpyDeviceToHost));
+            counters[0] = npairs;
+            counters[1] = h[0];
+            counters[2] = h[2];
+            counters[3] = 1;
+        }
+    }
+    return GBIVF_OK;
+}
+
 }  // extern "C"
 
 struct gbivf_graph {
@@ -966,6 +1093,23 @@ int gbivf_graph_launch(gbivf_graph* gr, void* stream) {
     if (!gr || !gr->exec) return fail(GBIVF_ERR_INVALID, "graph is NULL");
     DeviceGuard g(gr->ix->device);
     CK(cudaGraphLaunch(gr->exec, (cudaStream_t)stream));
+    return GBIVF_OK;
+}
+
+int gbivf_graph_kernel_count(const gbivf_graph* gr, int* kernels) {
+    if (!gr || !gr->graph || !kernels) return fail(GBIVF_ERR_INVALID, "NULL argument");
+    DeviceGuard g(gr->ix->device);
+    size_t n = 0;
+    CK(cudaGraphGetNodes(gr->graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) CK(cudaGraphGetNodes(gr->graph, nodes.data(), &n));
+    int k = 0;
+    for (size_t i = 0; i < n; i++) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nodes[i], &t));
+        k += t == cudaGraphNodeTypeKernel;
+    }
+    *kernels = k;
     return GBIVF_OK;
 }
 
@@ -1327,8 +1471,10 @@ int gbivf_pq_search(gbivf_index* ix, const float* queries, int nq, int k, float*
 // centroid distance block) lives in one file-scope device array of
 // GBIVF_NOALLOC_SCRATCH_BYTES. Every GPU that loads this library holds the
 // array until the process exits. The host resolves the array's device address
-// with cudaGetSymbolAddress once per device, on the first call made on that
-// device (so that first call should come before any stream capture).
+// with cudaGetSymbolAddress on the first call made on a device, and again on
+// the first call after that device's context was replaced (cudaDeviceReset,
+// a new primary context): the module, and with it the array, is loaded anew
+// in every context. Such a first call should come before any stream capture.
 // All calls share the array: calls that overlap on the GPU (other streams,
 // other threads) race on it. The kernels overwrite every scratch byte they
 // read, so nothing needs clearing between calls.
@@ -1340,7 +1486,49 @@ constexpr size_t kNoallocScratchBytes = (size_t)GBIVF_NOALLOC_SCRATCH_BYTES;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[128] = {};
+struct NoallocSlot {
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;  // the context the address belongs to
+};
+NoallocSlot g_noalloc[128];
+
+// scratch bytes of one call: the query norms (rounded up to 256 bytes), then the distance block
+size_t noalloc_need(int64_t nq, int C) {
+    return ((size_t)nq * sizeof(double) + 255) / 256 * 256 + (size_t)nq * C * sizeof(float);
+}
+
+// the largest batch whose scratch fits
+int64_t noalloc_max_queries(int C) {
+    int64_t nq = (int64_t)((kNoallocScratchBytes - 256) / (sizeof(double) + (size_t)C * sizeof(float)));
+    while (nq > 0 && noalloc_need(nq, C) > kNoallocScratchBytes) nq--;
+    while (noalloc_need(nq + 1, C) <= kNoallocScratchBytes) nq++;
+    return nq;
+}
+
+// Unique id of the calling thread's current context, from the driver (resolved through the
+// runtime, so the library needs no link against the driver library); 0 when unknown.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -1353,26 +1541,28 @@ extern "C" int gbivf_coarse_assign_noalloc(gbivf_index* ix, const float* d_queri
     if (!d_queries || !d_coaidx || !d_coadis) return fail(GBIVF_ERR_INVALID, "NULL device buffer");
     const DevIndex& dx = ix->dx;
     const size_t norm_bytes = ((size_t)nq * sizeof(double) + 255) / 256 * 256;
-    const size_t need = norm_bytes + (size_t)nq * dx.C * sizeof(float);
+    const size_t need = noalloc_need(nq, dx.C);
     if (need > kNoallocScratchBytes)
         return fail(GBIVF_ERR_UNSUPPORTED,
                     "nq=%d with coarsek=%d needs %zu scratch bytes; the no-allocation scratch holds %zu "
-                    "(at most %zu queries per call at this coarsek)",
-                    nq, dx.C, need, kNoallocScratchBytes,
-                    (kNoallocScratchBytes - 256) / (sizeof(double) + (size_t)dx.C * sizeof(float)));
+                    "(at most %lld queries per call at this coarsek)",
+                    nq, dx.C, need, kNoallocScratchBytes, (long long)noalloc_max_queries(dx.C));
     if (ix->device < 0 || ix->device >= 128) return fail(GBIVF_ERR_UNSUPPORTED, "device %d", ix->device);
     DeviceGuard g(ix->device);
     if (!g.ok) return fail(GBIVF_ERR_CUDA, "cudaSetDevice(%d) failed", ix->device);
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[ix->device]) {
+        NoallocSlot& slot = g_noalloc[ix->device];
+        const unsigned long long ctx = current_context_id();
+        if (!slot.ptr || ctx == 0 || ctx != slot.ctx_id) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-            g_noalloc_ptr[ix->device] = p;
+            slot.ptr = p;
+            slot.ctx_id = ctx;
         }
-        base = g_noalloc_ptr[ix->device];
+        base = slot.ptr;
     }
     double* qn = reinterpret_cast<double*>(base);
     float* dist = reinterpret_cast<float*>(static_cast<unsigned char*>(base) + norm_bytes);

@@ -13,6 +13,7 @@ enum ScanFlags : int {
     SCAN_OUT_PACKED = 8,    // write min(L, k) results at out_start[q] (core_gpu)
     SCAN_MIXED = 16,        // precision form: FP16 approximate tables, exact re-score of alpha*k
     SCAN_REFINE = 32,       // re-rank the kl ADC candidates by their refined reconstruction
+    SCAN_KEYS_ONLY = 64,    // persistent scan: hand off the best keys, their count and the k-th key only
 };
 
 // Device view of one index (all pointers in device memory).
@@ -68,6 +69,11 @@ struct ScanArgs {
     // the hand-off's list of each candidate (cand_id then holds its code row)
     int sel_mult = 1, sel_cap = 0;
     int32_t* cand_list = nullptr;
+    // persistent scan over a subset of the batch: queries qlist[0 .. *nqlist) (NULL: 0 .. nq-1)
+    const int32_t* qlist = nullptr;
+    const int* nqlist = nullptr;
+    // SCAN_KEYS_ONLY: per query the k-th best key when k were found, else KEY_MAX
+    unsigned long long* tau_out = nullptr;
 };
 
 // per-query shape of a (possibly uneven) batch
@@ -99,10 +105,44 @@ cudaError_t launch_scan(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
 // k or kl <= 1024) and its finalize kernel; `mid`, when given, is recorded between
 // the two; returns cudaErrorNotSupported when not applicable
 cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads,
-                                   cudaStream_t st, cudaEvent_t mid = nullptr);
+                                   cudaStream_t st, cudaEvent_t mid = nullptr, bool finalize = true);
+// the finalize kernel alone (order / re-score / re-rank the hand-off and write the results)
+cudaError_t launch_finalize(const DevIndex& ix, const ScanArgs& a, cudaStream_t st);
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
+
+// List-centric scan (scan_lists.cu): the (query, list) pairs of a batch grouped by list, G queries
+// per work item. Device workspace, sized by the host for nq queries, C lists and at most
+// max_pairs (query, probe) pairs.
+struct ListScanWork {
+    int* w0 = nullptr;        // nq: the first pass's probe count per query
+    int* pcnt = nullptr;      // C: pairs per list (zeroed at launch)
+    int* pbeg = nullptr;      // C + 1: first pair of each list
+    int* fill = nullptr;      // C: fill cursors
+    int* gbeg = nullptr;      // C + 1: first group of each list
+    int4* pairs = nullptr;    // max_pairs: (query, probe, position of the probe's first row, 0), by list
+    int4* groups = nullptr;   // max_pairs: (list, first pair, pairs, 0)
+    int* counters = nullptr;  // [0] groups, [1] work counter, [2] overflowed queries
+    unsigned long long* keysA = nullptr;  // nq x cand_stride: the first pass's best keys ...
+    int* cntA = nullptr;                  // ... and their count
+    unsigned long long* tau = nullptr;    // nq: the first pass's k-th key (KEY_MAX: fewer rows)
+    unsigned long long* ebuf = nullptr;   // nq x ecap: keys below tau from the list-centric pass ...
+    int* ecnt = nullptr;                  // ... and their count (may exceed ecap: overflow)
+    int ecap = 0;
+    int32_t* ovf = nullptr;   // nq: the queries whose buffer overflowed
+    int* err = nullptr;       // device error flag (a bounded wait ran out)
+    int* queue_a = nullptr;   // work counters of the first pass and of the overflow pass
+    int* queue_b = nullptr;
+    int beta = 2;             // the first pass scans each query's nearest probes until beta * k_sel rows
+};
+bool list_scan_supported(const DevIndex& ix, const ScanArgs& a);
+int list_scan_ecap(const ScanArgs& a);
+// The list-centric search pipeline up to the finalize hand-off (a.cand_*): planning, first pass,
+// grouping, the list-centric scan, selection and the overflow pass. ev (optional, 5 events) marks
+// its stages: first pass start/end, scan start/end, overflow pass start.
+cudaError_t launch_list_scan(const DevIndex& ix, const ScanArgs& a, const ListScanWork& w, int num_sms,
+                             cudaStream_t st, cudaEvent_t* ev);
 
 // [min, max] of n int32 values on the device, returned to the host (synchronises the stream)
 cudaError_t launch_id_range(const int32_t* ids, int64_t n, int* range, cudaStream_t st);

@@ -1,0 +1,670 @@
+// List-centric IVF-PQ scan: the (query, list) pairs of a batch grouped by
+// list, one work item per (list, group of queries).
+//
+// The reference scans list by list inside each query (sumidxtab2 per probe,
+// sequential/ivf_pq/ivf_search.cpp:182-203; the MPI pipeline dispatches the
+// same per-list unit, parallel/ivf_pq/ivf_search.cpp:178-228, and the Xeon Phi
+// variant per probe, phi2/ivf_pq/ivf_parallel.cpp:276-278). In a large batch
+// most code bytes belong to lists that many queries probe, so here one CTA
+// takes a list and G queries that probe it:
+//
+//   * the list's code rows stream once through shared memory (1-D bulk copies,
+//     16 KB tiles, double-buffered on mbarriers) for all G queries;
+//   * the G queries' m x 256 tables are interleaved, entry-major: the G values
+//     of one entry fill one 16-byte word (4 FP32 in the exact form, 8 FP16 in
+//     the precision form), so one 128-bit shared load serves G queries;
+//   * each (row, query) sum runs in the reference's order and arithmetic, bit
+//     for bit the value the query-centric kernel computes.
+//
+// Top-k without per-query state in the CTA: a first pass (the query-centric
+// kernel, SCAN_KEYS_ONLY) scans each query's nearest probes until it holds
+// 2 k_sel rows and hands off its k_sel best keys and the k_sel-th key tau_q.
+// Every key of the exact top-k_sel over all probes is <= tau_q, so the
+// list-centric pass appends only keys below tau_q, to a per-query buffer in
+// global memory. The select kernel takes the k_sel smallest of both sets
+// (exact radix select) and writes the finalize kernel's hand-off; a query
+// whose buffer overflowed is scanned again by the query-centric kernel.
+// Results are identical to the query-centric path's.
+#include <cuda_fp16.h>
+
+#include "block_topk.cuh"
+#include "exact_round.cuh"
+#include "f32x2.cuh"
+#include "scan_common.cuh"
+#include "tc_common.cuh"
+
+namespace gbivf {
+
+constexpr int LC_NT = 512;        // threads of the list-centric scan (one CTA per SM)
+constexpr int LC_TILE = 16384;    // bytes of code rows per staged tile
+constexpr int LC_SEL_NT = 256;    // threads of the select kernel (one CTA per query)
+
+template <bool MIXED>
+struct LcShape {
+    static constexpr int G = MIXED ? 8 : 4;  // queries per work item: one 16-byte table word
+};
+
+__device__ __forceinline__ int lc_ksel(const ScanArgs& a, int q) {
+    const int kq0 = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : query_k(a, q);
+    return (a.flags & SCAN_MIXED) ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
+}
+
+// ---------------------------------------------------------------------------
+// planning: prefix probes per query, pairs per list, groups
+// ---------------------------------------------------------------------------
+
+// One warp per query: the first pass's probe count p_q (the fewest leading probes holding
+// beta * k_sel rows, all of them when the query has fewer), and one count per remaining
+// non-empty probe on its list. Zeroes the query's emission counter.
+__global__ void lc_plan_kernel(DevIndex ix, ScanArgs a, ListScanWork w, int beta) {
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (q >= a.nq) return;
+    const int wq = query_w(a, q);
+    const int64_t target = (int64_t)beta * lc_ksel(a, q);
+    int64_t carry = 0;
+    int p = wq;
+    for (int j0 = 0; j0 < wq && p == wq; j0 += 32) {
+        const int j = j0 + lane;
+        const int l = j < wq ? __ldg(a.probes + (int64_t)q * a.w + j) : -1;
+        int64_t incl = l >= 0 ? __ldg(ix.list_len + l) : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, j < wq && carry + incl >= target);
+        if (hit) p = j0 + __ffs(hit);  // probes 0 .. j0 + ffs - 1
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) {
+        w.w0[q] = p;
+        w.ecnt[q] = 0;
+    }
+    for (int j = p + lane; j < wq; j += 32) {
+        const int l = __ldg(a.probes + (int64_t)q * a.w + j);
+        if (l >= 0 && __ldg(ix.list_len + l) > 0) atomicAdd(&w.pcnt[l], 1);
+    }
+}
+
+// One block: exclusive prefix sums over the C lists of the pair counts (pbeg) and of the groups
+// of G pairs (gbeg); fill cursors start at pbeg; the totals go to pbeg[C], gbeg[C], counters[0].
+template <int G>
+__global__ void __launch_bounds__(1024) lc_prefix_kernel(int C, ListScanWork w) {
+    __shared__ int s_p[1024], s_g[1024];
+    const int tid = threadIdx.x, per = (C + 1023) / 1024;
+    const int b = min(C, tid * per), e = min(C, b + per);
+    int sp = 0, sg = 0;
+    for (int l = b; l < e; l++) {
+        const int c = w.pcnt[l];
+        sp += c;
+        sg += (c + G - 1) / G;
+    }
+    s_p[tid] = sp;
+    s_g[tid] = sg;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+        const int vp = tid >= o ? s_p[tid - o] : 0, vg = tid >= o ? s_g[tid - o] : 0;
+        __syncthreads();
+        s_p[tid] += vp;
+        s_g[tid] += vg;
+        __syncthreads();
+    }
+    int rp = s_p[tid] - sp, rg = s_g[tid] - sg;
+    for (int l = b; l < e; l++) {
+        const int c = w.pcnt[l];
+        w.pbeg[l] = rp;
+        w.fill[l] = rp;
+        w.gbeg[l] = rg;
+        rp += c;
+        rg += (c + G - 1) / G;
+    }
+    if (tid == 1023) {
+        w.pbeg[C] = s_p[1023];
+        w.gbeg[C] = s_g[1023];
+        w.counters[0] = s_g[1023];
+    }
+}
+
+// One warp per query: the position of each probe's first row in the query's candidate order (the
+// prefix of list lengths over all its probes) and a pair record per probe the first pass left.
+__global__ void lc_fill_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (q >= a.nq) return;
+    const int wq = query_w(a, q), p = w.w0[q];
+    uint32_t carry = 0;
+    for (int j0 = 0; j0 < wq; j0 += 32) {
+        const int j = j0 + lane;
+        const int l = j < wq ? __ldg(a.probes + (int64_t)q * a.w + j) : -1;
+        const uint32_t len = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
+        uint32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (j >= p && j < wq && len > 0) {
+            const int slot = atomicAdd(&w.fill[l], 1);
+            w.pairs[slot] = make_int4(q, j, (int)(carry + incl - len), 0);
+        }
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+// One thread per list: its groups of up to G pairs.
+template <int G>
+__global__ void lc_groups_kernel(int C, ListScanWork w) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= C) return;
+    const int pb = w.pbeg[l], n = w.pbeg[l + 1] - pb, g0 = w.gbeg[l];
+    for (int g = 0; g * G < n; g++) w.groups[g0 + g] = make_int4(l, pb + g * G, min(G, n - g * G), 0);
+}
+
+// ---------------------------------------------------------------------------
+// the list-centric scan
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t lc_byte(uint32_t v, int s) { return __byte_perm(v, 0u, 0x4440u | (uint32_t)s); }
+
+__device__ __forceinline__ float lc_add_h(float acc, uint32_t word, int hi) {
+    const unsigned short h = (unsigned short)(hi ? (word >> 16) : (word & 0xffffu));
+    asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc) : "h"(h));
+    return acc;
+}
+
+template <int M, bool MIXED>
+__global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
+    constexpr int NT = LC_NT, D = 128, KS = 256, DS = D / M;
+    constexpr int G = LcShape<MIXED>::G;
+    constexpr int TPS = NT / M;       // threads per sub-quantizer
+    constexpr int E = KS / TPS;       // entries per thread: c = (tid % TPS) + TPS * i
+    constexpr int GR = 16 / M;        // code rows per 16-byte group
+    constexpr int TILE_GROUPS = LC_TILE / 16;
+    constexpr int TILE_ROWS = LC_TILE / M;
+    constexpr int UG = TILE_GROUPS / NT;  // 16-byte groups per thread per tile
+    static_assert(E % 2 == 0 && E * TPS == KS && UG * NT == TILE_GROUPS, "shape");
+    static_assert(G * GR <= 32, "pass bits of a group fit one word");
+
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint4* stage = reinterpret_cast<uint4*>(smem);                       // 2 x LC_TILE
+    unsigned char* tab = smem + 2 * LC_TILE;                             // M x 256 x 16 bytes
+    float* rr = reinterpret_cast<float*>(tab + M * KS * 16);             // G x D residuals
+    float* rn = rr + G * D;                                              // G x M sub-norms
+    __shared__ int s_q[G];
+    __shared__ uint32_t s_pos0[G];
+    __shared__ u64 s_tau[G];
+    __shared__ int s_next, s_abort;
+    __shared__ __align__(8) uint64_t bar[2];
+
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int my_s = tid / TPS, my_cl = tid % TPS;
+
+    // this thread's slice of the codebook: entries (my_s, my_cl + TPS * i), i < E
+    constexpr int EP = MIXED ? 1 : E, EM = MIXED ? E / 2 : 1;
+    float cen[EP][DS];
+    float nhi[EP], nlo[EP];
+    f2_t cen2[EM][DS], cn2[EM];
+#pragma unroll
+    for (int i = 0; i < (MIXED ? 0 : E); i++) {
+        const int e = my_s * KS + my_cl + TPS * i;
+        const float4* src = reinterpret_cast<const float4*>(ix.pq + (int64_t)e * DS);
+#pragma unroll
+        for (int v = 0; v < DS / 4; v++) {
+            const float4 x = __ldg(src + v);
+            cen[i][4 * v] = x.x;
+            cen[i][4 * v + 1] = x.y;
+            cen[i][4 * v + 2] = x.z;
+            cen[i][4 * v + 3] = x.w;
+        }
+        nhi[i] = __ldg(ix.pq_hi + e);
+        nlo[i] = __ldg(ix.pq_lo + e);
+    }
+#pragma unroll
+    for (int p = 0; p < (MIXED ? EM : 0); p++) {
+        const int e0 = my_s * KS + my_cl + TPS * (2 * p), e1 = e0 + TPS;
+        const float4* s0 = reinterpret_cast<const float4*>(ix.pq + (int64_t)e0 * DS);
+        const float4* s1 = reinterpret_cast<const float4*>(ix.pq + (int64_t)e1 * DS);
+#pragma unroll
+        for (int v = 0; v < DS / 4; v++) {
+            const float4 x = __ldg(s0 + v), y = __ldg(s1 + v);
+            cen2[p][4 * v] = f2_pack(x.x, y.x);
+            cen2[p][4 * v + 1] = f2_pack(x.y, y.y);
+            cen2[p][4 * v + 2] = f2_pack(x.z, y.z);
+            cen2[p][4 * v + 3] = f2_pack(x.w, y.w);
+        }
+        cn2[p] = f2_pack(0.25f * __ldg(ix.pq_hi + e0), 0.25f * __ldg(ix.pq_hi + e1));
+    }
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_next = atomicAdd(&w.counters[1], 1);
+        s_abort = 0;
+    }
+    const int ngroups = w.counters[0];
+    uint32_t phase = 0;   // bit s: the parity the next wait on stage s expects
+    uint32_t tc = 0;      // tiles consumed so far: tile tc uses stage tc & 1
+    bool armed[2] = {false, false};
+
+    for (;;) {
+        __syncthreads();  // the previous item's table and stages are no longer read
+        const int gi = s_next;
+        if (gi >= ngroups || s_abort) break;
+        const int4 gd = w.groups[gi];
+        const int l = gd.x, pb = gd.y, np = gd.z;
+        const int len = __ldg(ix.list_len + l);
+        const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
+        const int nbytes = (len * M + 15) & ~15;  // the code array is padded to whole 16-byte groups
+        const int ntiles = (nbytes + LC_TILE - 1) / LC_TILE;
+        if (tid < G) {
+            if (tid < np) {
+                const int4 pr = w.pairs[pb + tid];
+                s_q[tid] = pr.x;
+                s_pos0[tid] = (uint32_t)pr.z;
+                s_tau[tid] = w.tau[pr.x];
+            } else {
+                s_q[tid] = -1;
+                s_pos0[tid] = 0u;
+                s_tau[tid] = 0ull;  // nothing passes
+            }
+        }
+        if (tid == 0) {
+            s_next = atomicAdd(&w.counters[1], 1);
+            const int st = tc & 1;
+            mbar_expect_tx(&bar[st], (uint32_t)min(nbytes, LC_TILE));
+            bulk_load(stage + st * TILE_GROUPS, codes, (uint32_t)min(nbytes, LC_TILE), &bar[st]);
+            armed[st] = true;
+        }
+        __syncthreads();
+        // residuals r_g = x_q - y_l (bsxfunMINUS, ivf_search.cpp:155-172)
+        for (int e = tid; e < G * D; e += NT) {
+            const int g = e / D, x = e % D;
+            rr[e] = g < np ? __fsub_rn(__ldg(a.queries + (int64_t)s_q[g] * D + x), __ldg(ix.coa + (int64_t)l * D + x))
+                           : 0.0f;
+        }
+        __syncthreads();
+        for (int e = tid; e < np * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
+        __syncthreads();
+        // the G interleaved tables from the register codebook
+        if constexpr (MIXED) {
+            // ||r_s - c||^2 / 4 = ||r_s||^2 / 4 + ||c||^2 / 4 - <r_s, c> / 2 by packed fused multiply-adds, in FP16
+            uint32_t hw[G][EM];
+#pragma unroll
+            for (int g = 0; g < G; g++) {
+                if (g < np) {
+                    f2_t rs2[DS];
+                    const float4* r4 = reinterpret_cast<const float4*>(rr + g * D + my_s * DS);
+#pragma unroll
+                    for (int v4 = 0; v4 < DS / 4; v4++) {
+                        const float4 x = r4[v4];
+                        rs2[4 * v4] = f2_pack(x.x, x.x);
+                        rs2[4 * v4 + 1] = f2_pack(x.y, x.y);
+                        rs2[4 * v4 + 2] = f2_pack(x.z, x.z);
+                        rs2[4 * v4 + 3] = f2_pack(x.w, x.w);
+                    }
+                    const float f4 = 0.25f * rn[g * M + my_s];
+                    const f2_t f42 = f2_pack(f4, f4), mh2 = f2_pack(-0.5f, -0.5f);
+#pragma unroll
+                    for (int p = 0; p < EM; p++) {
+                        f2_t dt = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                        for (int t = 0; t < DS; t++) dt = f2_fma(rs2[t], cen2[p][t], dt);
+                        float e0, e1;
+                        f2_unpack(f2_fma(mh2, dt, f2_add(f42, cn2[p])), e0, e1);
+                        uint32_t r;
+                        asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(e1), "f"(e0));
+                        hw[g][p] = r;  // (entry 2p, entry 2p+1) of query g
+                    }
+                } else {
+#pragma unroll
+                    for (int p = 0; p < EM; p++) hw[g][p] = 0u;
+                }
+            }
+            // entry-major words: the 8 queries' FP16 values of one entry in one 16-byte word
+#pragma unroll
+            for (int p = 0; p < EM; p++) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const uint32_t sel = h ? 0x7632u : 0x5410u;
+                    const uint4 v = make_uint4(__byte_perm(hw[0][p], hw[1][p], sel), __byte_perm(hw[2][p], hw[3][p], sel),
+                                               __byte_perm(hw[4][p], hw[5][p], sel), __byte_perm(hw[6][p], hw[7][p], sel));
+                    const int c = my_cl + TPS * (2 * p + h);
+                    *reinterpret_cast<uint4*>(tab + ((my_s * KS + c) << 4)) = v;
+                }
+            }
+        } else {
+            // the reference's entry: -2 <r_s, c> + (float)(||c||^2 + ||r_s||^2) (nn.c:113-150), the dot
+            // product's products as fma(r, c, -0) (one rounding, never fused with the add)
+            float out[G][E];
+            const f2_t m2 = f2_pack(-2.0f, -2.0f), nz2 = f2_pack(a.neg_zero, a.neg_zero);
+#pragma unroll
+            for (int g = 0; g < G; g++) {
+                if (g < np) {
+                    float rs[DS];
+                    const float4* r4 = reinterpret_cast<const float4*>(rr + g * D + my_s * DS);
+#pragma unroll
+                    for (int v4 = 0; v4 < DS / 4; v4++) {
+                        const float4 x = r4[v4];
+                        rs[4 * v4] = x.x;
+                        rs[4 * v4 + 1] = x.y;
+                        rs[4 * v4 + 2] = x.z;
+                        rs[4 * v4 + 3] = x.w;
+                    }
+                    const float f = rn[g * M + my_s];
+                    const f2_t f2 = f2_pack(f, f);
+#pragma unroll
+                    for (int i = 0; i < E; i += 2) {
+                        f2_t d2 = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                        for (int t = 0; t < DS; t++)
+                            d2 = f2_add(d2, f2_fma(f2_pack(rs[t], rs[t]), f2_pack(cen[i][t], cen[i + 1][t]), nz2));
+                        float d0, d1;
+                        f2_unpack(d2, d0, d1);
+                        const f2_t hi2 = f2_pack(nhi[i], nhi[i + 1]);
+                        const f2_t S2 = f2_add(hi2, f2);
+                        const f2_t bb = f2_sub(S2, hi2);
+                        const f2_t e1 = f2_add(f2_sub(hi2, f2_sub(S2, bb)), f2_sub(f2, bb));
+                        const f2_t t2 = f2_add(e1, f2_pack(nlo[i], nlo[i + 1]));
+                        float Sa, Sb, ta, tb;
+                        f2_unpack(S2, Sa, Sb);
+                        f2_unpack(t2, ta, tb);
+                        const int e = my_s * KS + my_cl + TPS * i;
+                        const f2_t c02 = f2_pack(add_norms_finish(ix.pq_norm + e, Sa, ta, f),
+                                                 add_norms_finish(ix.pq_norm + e + TPS, Sb, tb, f));
+                        f2_unpack(f2_add(f2_mul(m2, f2_pack(d0, d1)), c02), out[g][i], out[g][i + 1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < E; i++) out[g][i] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < E; i++) {
+                const int c = my_cl + TPS * i;
+                *reinterpret_cast<float4*>(tab + ((my_s * KS + c) << 4)) =
+                    make_float4(out[0][i], out[1][i], out[2][i], out[3][i]);
+            }
+        }
+        int qg[G];
+        uint32_t pos0[G];
+        u64 tau[G];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            qg[g] = s_q[g];
+            pos0[g] = s_pos0[g];
+            tau[g] = s_tau[g];
+        }
+        __syncthreads();  // tables written
+
+        for (int t = 0; t < ntiles; t++, tc++) {
+            const int st = tc & 1;
+            const bool ok = mbar_wait(&bar[st], (phase >> st) & 1u);
+            if (__syncthreads_or(!ok)) {  // a copy did not land in time: report, drain, stop
+                if (tid == 0) {
+                    s_abort = 1;
+                    atomicOr(w.err, 1);
+                }
+                goto done;
+            }
+            phase ^= 1u << st;
+            armed[st] = false;
+            if (tid == 0 && t + 1 < ntiles) {
+                const int nb = min(LC_TILE, nbytes - (t + 1) * LC_TILE);
+                mbar_expect_tx(&bar[st ^ 1], (uint32_t)nb);
+                bulk_load(stage + (st ^ 1) * TILE_GROUPS, codes + (int64_t)(t + 1) * LC_TILE, (uint32_t)nb,
+                          &bar[st ^ 1]);
+                armed[st ^ 1] = true;
+            }
+            const uint4* sg = stage + st * TILE_GROUPS;
+            const int row0 = t * TILE_ROWS;
+            const int ngt = min(TILE_GROUPS, (min(TILE_ROWS, len - row0) * M + 15) / 16);
+#pragma unroll
+            for (int u = 0; u < UG; u++) {
+                const int gl = u * NT + tid;
+                if (u * NT + (tid & ~31) >= ngt) break;  // warp-uniform
+                const uint4 c = gl < ngt ? sg[gl] : make_uint4(0, 0, 0, 0);
+                const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+                float acc[GR][G];
+                uint32_t pass = 0;
+#pragma unroll
+                for (int r = 0; r < GR; r++) {
+                    const int row = row0 + gl * GR + r;
+                    if constexpr (MIXED) {
+                        float s8[G];
+#pragma unroll
+                        for (int g = 0; g < G; g++) s8[g] = 0.0f;
+#pragma unroll
+                        for (int s = 0; s < M; s++) {
+                            const uint32_t b = lc_byte(cw[(r * M + s) >> 2], (r * M + s) & 3);
+                            const uint4 v = *reinterpret_cast<const uint4*>(tab + ((s * KS + b) << 4));
+                            const uint32_t vw[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                            for (int g = 0; g < G; g++) s8[g] = lc_add_h(s8[g], vw[g >> 1], g & 1);
+                        }
+#pragma unroll
+                        for (int g = 0; g < G; g++) acc[r][g] = s8[g] * 4.0f;
+                    } else {
+                        f2_t a01 = f2_pack(0.0f, 0.0f), a23 = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                        for (int s = 0; s < M; s++) {
+                            const uint32_t b = lc_byte(cw[(r * M + s) >> 2], (r * M + s) & 3);
+                            const float4 v = *reinterpret_cast<const float4*>(tab + ((s * KS + b) << 4));
+                            a01 = f2_add(a01, f2_pack(v.x, v.y));
+                            a23 = f2_add(a23, f2_pack(v.z, v.w));
+                        }
+                        f2_unpack(a01, acc[r][0], acc[r][1]);
+                        f2_unpack(a23, acc[r][2], acc[r][3]);
+                    }
+                    const bool valid = gl < ngt && row < len;
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        const u64 key = make_key(acc[r][g], pos0[g] + (uint32_t)row);
+                        if (valid && key < tau[g]) pass |= 1u << (g * GR + r);
+                    }
+                }
+                if (__any_sync(0xffffffffu, pass != 0)) {
+                    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        unsigned msk[GR];
+                        int tot = 0;
+#pragma unroll
+                        for (int r = 0; r < GR; r++) {
+                            msk[r] = __ballot_sync(0xffffffffu, (pass >> (g * GR + r)) & 1u);
+                            tot += __popc(msk[r]);
+                        }
+                        if (tot == 0) continue;  // warp-uniform
+                        int base = 0;
+                        if (lane == 0) base = atomicAdd(&w.ecnt[qg[g]], tot);
+                        base = __shfl_sync(0xffffffffu, base, 0);
+                        u64* out = w.ebuf + (int64_t)qg[g] * w.ecap;
+#pragma unroll
+                        for (int r = 0; r < GR; r++) {
+                            if ((pass >> (g * GR + r)) & 1u) {
+                                const int idx = base + __popc(msk[r] & lt);
+                                if (idx < w.ecap)
+                                    out[idx] = make_key(acc[r][g], pos0[g] + (uint32_t)(row0 + gl * GR + r));
+                            }
+                            base += __popc(msk[r]);
+                        }
+                    }
+                }
+            }
+            __syncthreads();  // this stage is free again
+        }
+    }
+done:
+    // let every copy in flight land before the CTA's shared memory goes away (bounded waits)
+    if (tid == 0)
+        for (int s = 0; s < 2; s++)
+            if (armed[s]) mbar_wait(&bar[s], (phase >> s) & 1u);
+}
+
+// ---------------------------------------------------------------------------
+// selection: the first pass's best keys and the emitted keys -> the finalize hand-off
+// ---------------------------------------------------------------------------
+
+template <bool ROWS_OUT>
+__global__ void __launch_bounds__(LC_SEL_NT) lc_select_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int q = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    const int na = w.cntA[q], ne = w.ecnt[q];
+    if (ne > w.ecap) {  // the buffer overflowed: the query-centric kernel scans this query again
+        if (tid == 0) w.ovf[atomicAdd(&w.counters[2], 1)] = q;
+        return;
+    }
+    const int stride = a.cand_stride, wq = query_w(a, q);
+    u64* pool = reinterpret_cast<u64*>(smem);                            // na + ne keys
+    uint32_t* prefix = reinterpret_cast<uint32_t*>(pool + stride + w.ecap);  // wq + 1
+    int* plist = reinterpret_cast<int*>(prefix + a.w + 1);                // wq
+    unsigned char* work = reinterpret_cast<unsigned char*>(plist + a.w + 1);
+    work = reinterpret_cast<unsigned char*>(((uintptr_t)work + 15) & ~(uintptr_t)15);
+    __shared__ int s_cnt;
+    TopKSmem s{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0, work};
+    for (int i = tid; i < na; i += LC_SEL_NT) pool[i] = w.keysA[(int64_t)q * stride + i];
+    for (int i = tid; i < ne; i += LC_SEL_NT) pool[na + i] = w.ebuf[(int64_t)q * w.ecap + i];
+    for (int j = tid; j < wq; j += LC_SEL_NT) {
+        const int l = __ldg(a.probes + (int64_t)q * a.w + j);
+        plist[j] = l;
+        prefix[j] = l >= 0 ? (uint32_t)__ldg(ix.list_len + l) : 0u;
+    }
+    if (tid == 0) {
+        s_cnt = 0;
+        s.slots()[0] = 0;
+    }
+    __syncthreads();
+    if (tid < 32) {  // exclusive prefix of the probe lengths
+        uint32_t carry = 0;
+        for (int j0 = 0; j0 < wq; j0 += 32) {
+            const int j = j0 + lane;
+            const uint32_t len = j < wq ? prefix[j] : 0u;
+            uint32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (j < wq) prefix[j] = carry + incl - len;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) prefix[wq] = carry;
+    }
+    const int n = na + ne, K = min(lc_ksel(a, q), n);
+    u64 T = KEY_MAX;
+    if (n > K && K > 0) T = block_kth(s, pool, n, pool, 0, K);  // the K-th smallest key
+    __syncthreads();
+    const int64_t o0 = (int64_t)q * stride;
+    for (int i0 = 0; i0 < n; i0 += LC_SEL_NT) {
+        const int i = i0 + tid;
+        const u64 key = i < n ? pool[i] : KEY_MAX;
+        const bool keep = i < n && key <= T && K > 0;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (!m) continue;
+        int base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(&s_cnt, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+        if (keep) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            const uint32_t pos = key_payload(key);
+            const int j = probe_of(prefix, wq, pos);
+            const int l = plist[j];
+            const int64_t row = ix.list_beg[l] + (int64_t)(pos - prefix[j]);
+            a.cand_key[o0 + slot] = key;
+            if (ROWS_OUT) {
+                a.cand_id[o0 + slot] = (int32_t)row;
+                a.cand_list[o0 + slot] = l;
+            } else {
+                a.cand_id[o0 + slot] = ix.ids[row];
+            }
+        }
+    }
+    for (int c = K + tid; c < stride; c += LC_SEL_NT) {
+        a.cand_key[o0 + c] = KEY_MAX;
+        a.cand_id[o0 + c] = -1;
+        if (ROWS_OUT) a.cand_list[o0 + c] = 0;
+    }
+    if (tid == 0) a.cand_cnt[q] = K;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+bool list_scan_supported(const DevIndex& ix, const ScanArgs& a) {
+    return scan_persistent_supported(ix, a) && !(a.flags & (SCAN_TABLE_DIRECT | SCAN_SRC_RESIDUAL | SCAN_OUT_PACKED));
+}
+
+int list_scan_ecap(const ScanArgs& a) { return 2 * scan_persistent_stride(a) + 2048; }
+
+template <int M, bool MIXED>
+static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListScanWork& w, int num_sms,
+                             cudaStream_t st, cudaEvent_t* ev) {
+    constexpr int G = LcShape<MIXED>::G;
+    const int C = ix.C, nq = a.nq;
+    cudaError_t e;
+    auto rec = [&](int i) { return ev && ev[i] ? cudaEventRecord(ev[i], st) : cudaSuccess; };
+    if ((e = cudaMemsetAsync(w.pcnt, 0, sizeof(int) * C, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(w.counters, 0, sizeof(int) * 3, st)) != cudaSuccess) return e;
+    const int wblocks = (nq * 32 + 255) / 256;
+    lc_plan_kernel<<<wblocks, 256, 0, st>>>(ix, a, w, std::max(1, w.beta));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // first pass: the query-centric kernel over each query's leading probes, keys only
+    ScanArgs pa = a;
+    pa.flags |= SCAN_KEYS_ONLY;
+    pa.w_per_q = w.w0;
+    pa.cand_key = w.keysA;
+    pa.cand_cnt = w.cntA;
+    pa.cand_id = nullptr;
+    pa.cand_list = nullptr;
+    pa.tau_out = w.tau;
+    pa.queue = w.queue_a;
+    if ((e = rec(0)) != cudaSuccess) return e;
+    if ((e = launch_scan_persistent(ix, pa, num_sms, 512, st, nullptr, false)) != cudaSuccess) return e;
+    if ((e = rec(1)) != cudaSuccess) return e;
+    lc_prefix_kernel<G><<<1, 1024, 0, st>>>(C, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    lc_fill_kernel<<<wblocks, 256, 0, st>>>(ix, a, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    lc_groups_kernel<G><<<(C + 255) / 256, 256, 0, st>>>(C, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = rec(2)) != cudaSuccess) return e;
+    const size_t smem = 2 * LC_TILE + (size_t)M * 256 * 16 + sizeof(float) * (G * 128 + G * M);
+    auto kern = lc_scan_kernel<M, MIXED>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
+    kern<<<num_sms, LC_NT, smem, st>>>(ix, a, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = rec(3)) != cudaSuccess) return e;
+    const bool rows_out = (a.flags & (SCAN_MIXED | SCAN_REFINE)) != 0;
+    const size_t ssm = sizeof(u64) * ((size_t)a.cand_stride + w.ecap) + sizeof(int) * (2 * (size_t)a.w + 2) + 16 +
+                       TOPK_WORK_BYTES;
+    void (*sel)(DevIndex, ScanArgs, ListScanWork) = rows_out ? lc_select_kernel<true> : lc_select_kernel<false>;
+    if ((e = cudaFuncSetAttribute(sel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm)) != cudaSuccess)
+        return e;
+    sel<<<nq, LC_SEL_NT, ssm, st>>>(ix, a, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // queries whose buffer overflowed: the query-centric kernel, all their probes, full hand-off
+    ScanArgs fa = a;
+    fa.qlist = w.ovf;
+    fa.nqlist = w.counters + 2;
+    fa.queue = w.queue_b;
+    if ((e = rec(4)) != cudaSuccess) return e;
+    return launch_scan_persistent(ix, fa, num_sms, 512, st, nullptr, false);
+}
+
+cudaError_t launch_list_scan(const DevIndex& ix, const ScanArgs& a, const ListScanWork& w, int num_sms,
+                             cudaStream_t st, cudaEvent_t* ev) {
+    if (a.nq <= 0) return cudaSuccess;
+    if (!list_scan_supported(ix, a) || ix.C > (1 << 24)) return cudaErrorNotSupported;
+    if (w.ecap < 1 || w.ecap > list_scan_ecap(a)) return cudaErrorInvalidValue;
+    const bool mixed = a.flags & SCAN_MIXED;
+    switch (ix.m) {
+        case 4: return mixed ? launch_lc<4, true>(ix, a, w, num_sms, st, ev) : launch_lc<4, false>(ix, a, w, num_sms, st, ev);
+        case 8: return mixed ? launch_lc<8, true>(ix, a, w, num_sms, st, ev) : launch_lc<8, false>(ix, a, w, num_sms, st, ev);
+        case 16:
+            return mixed ? launch_lc<16, true>(ix, a, w, num_sms, st, ev) : launch_lc<16, false>(ix, a, w, num_sms, st, ev);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+}  // namespace gbivf

@@ -201,10 +201,13 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
     }
 
     if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);
+    // the batch, or the subset of it that a.qlist names (its count written by an earlier kernel)
+    const int nwork = a.qlist ? *a.nqlist : a.nq;
     for (;;) {
         __syncthreads();
-        const int q = qslot[1];
-        if (q >= a.nq) break;
+        const int qi = qslot[1];
+        if (qi >= nwork) break;
+        const int q = a.qlist ? a.qlist[qi] : qi;
         // this query's probe count and result count (uneven batches)
         const int wq = query_w(a, q);
         // its probe lists and their lengths, loaded by all threads at once (one memory round trip
@@ -492,6 +495,16 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
             topk_flush(s, nb);
         }
         const int nbest = *s.nbest;
+        if (a.flags & SCAN_KEYS_ONLY) {
+            // the best keys, unordered, their count, and the k-th best key (the bound of the rows not
+            // scanned here: the list-centric pass keeps only rows below it)
+            for (int c = tid; c < nbest; c += NT) a.cand_key[(int64_t)q * a.cand_stride + c] = best[c];
+            if (tid == 0) {
+                a.cand_cnt[q] = nbest;
+                a.tau_out[q] = nbest == kq ? *s.thresh : KEY_MAX;
+            }
+            continue;
+        }
         if (rows_out) {
             // The code row and its list of each candidate, for the exact re-score or the refinement
             // re-rank, grouped by probe (a counting sort on probe & 255): neighbouring threads of the
@@ -820,12 +833,41 @@ int scan_persistent_stride(const ScanArgs& a) {
     return pow2_at_least(std::max(std::max(sel, a.k), 2));
 }
 
+template <int M, bool MIXED>
+static cudaError_t launch_fin(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
+    const size_t fsm = (size_t)a.cand_stride * 12 + 512;  // keys, ids, the query
+    const bool big = !MIXED && (a.flags & SCAN_REFINE);
+    void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
+    if constexpr (!MIXED)
+        if (big) fin = finalize_kernel<false, M, FIN_NT_BIG>;
+    if (fsm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+        if (e != cudaSuccess) return e;
+    }
+    fin<<<a.nq, big ? FIN_NT_BIG : FIN_NT, fsm, st>>>(ix, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
+    if (a.nq <= 0) return cudaSuccess;
+    const bool mixed = a.flags & SCAN_MIXED;
+    switch (ix.m) {
+        case 4: return mixed ? launch_fin<4, true>(ix, a, st) : launch_fin<4, false>(ix, a, st);
+        case 8: return mixed ? launch_fin<8, true>(ix, a, st) : launch_fin<8, false>(ix, a, st);
+        case 16: return mixed ? launch_fin<16, true>(ix, a, st) : launch_fin<16, false>(ix, a, st);
+        default: return cudaErrorNotSupported;
+    }
+}
+
 template <int M, bool DIRECT, int NT, bool MIXED = false>
-static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid) {
+static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid,
+                             bool finalize) {
     const int kcap = scan_persistent_stride(a);
-    if (a.cand_stride != kcap || !a.cand_key || !a.cand_id || !a.cand_cnt) return cudaErrorInvalidValue;
-    if (MIXED && (!a.cand_list || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
-    if ((a.flags & SCAN_REFINE) && (!a.cand_list || !ix.codes2 || !ix.pq2)) return cudaErrorInvalidValue;
+    const bool keys_only = a.flags & SCAN_KEYS_ONLY;
+    if (a.cand_stride != kcap || !a.cand_key || (!a.cand_id && !keys_only) || !a.cand_cnt) return cudaErrorInvalidValue;
+    if (MIXED && ((!a.cand_list && !keys_only) || a.sel_mult < 1 || a.sel_cap < 1)) return cudaErrorInvalidValue;
+    if ((a.flags & SCAN_REFINE) && ((!a.cand_list && !keys_only) || !ix.codes2 || !ix.pq2)) return cudaErrorInvalidValue;
+    if (a.qlist && !a.nqlist) return cudaErrorInvalidValue;
     ScanSmem L = scan_smem_layout(M, 256, 128, a.w, kcap, SP_BCAP, 2, SP_RCH, MIXED ? 2 : 4,
                                   MIXED ? (size_t)SP_NS * std::min((M == 4 ? 1 : 2) * NT, 1024) * 16 : 0);
     auto kern = ivf_scan_persistent_kernel<M, DIRECT, NT, MIXED>;
@@ -835,53 +877,47 @@ static cudaError_t launch_sp(const DevIndex& ix, const ScanArgs& a, int num_sms,
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, L.total);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    const int grid = std::min(a.nq, num_sms * per_sm);
+    const int grid = a.qlist ? num_sms * per_sm : std::min(a.nq, num_sms * per_sm);
     e = cudaMemsetAsync(a.queue, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     kern<<<grid, NT, L.total, st>>>(ix, a, L, kcap);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (!finalize) return cudaSuccess;
     if (mid && (e = cudaEventRecord(mid, st)) != cudaSuccess) return e;
-    const size_t fsm = (size_t)a.cand_stride * 12 + 512;  // keys, ids, the query
-    const bool big = !MIXED && (a.flags & SCAN_REFINE);
-    void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
-    if constexpr (!MIXED)
-        if (big) fin = finalize_kernel<false, M, FIN_NT_BIG>;
-    if (fsm > 48 * 1024) {
-        e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
-        if (e != cudaSuccess) return e;
-    }
-    fin<<<a.nq, big ? FIN_NT_BIG : FIN_NT, fsm, st>>>(ix, a);
-    return cudaGetLastError();
+    return launch_fin<M, MIXED>(ix, a, st);
 }
 
 template <int NT>
-static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid) {
+static cudaError_t launch_sp_nt(const DevIndex& ix, const ScanArgs& a, int num_sms, cudaStream_t st, cudaEvent_t mid,
+                                bool fin) {
     const bool direct = a.flags & SCAN_TABLE_DIRECT;
     if (a.flags & SCAN_MIXED) {  // the precision form: expansion tables only
         if (direct) return cudaErrorNotSupported;
         switch (ix.m) {
-            case 4: return launch_sp<4, false, NT, true>(ix, a, num_sms, st, mid);
-            case 8: return launch_sp<8, false, NT, true>(ix, a, num_sms, st, mid);
-            default: return launch_sp<16, false, NT, true>(ix, a, num_sms, st, mid);
+            case 4: return launch_sp<4, false, NT, true>(ix, a, num_sms, st, mid, fin);
+            case 8: return launch_sp<8, false, NT, true>(ix, a, num_sms, st, mid, fin);
+            default: return launch_sp<16, false, NT, true>(ix, a, num_sms, st, mid, fin);
         }
     }
     switch (ix.m) {
         case 4:
-            return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st, mid) : launch_sp<4, false, NT>(ix, a, num_sms, st, mid);
+            return direct ? launch_sp<4, true, NT>(ix, a, num_sms, st, mid, fin) : launch_sp<4, false, NT>(ix, a, num_sms, st, mid, fin);
         case 8:
-            return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st, mid) : launch_sp<8, false, NT>(ix, a, num_sms, st, mid);
+            return direct ? launch_sp<8, true, NT>(ix, a, num_sms, st, mid, fin) : launch_sp<8, false, NT>(ix, a, num_sms, st, mid, fin);
         default:
-            return direct ? launch_sp<16, true, NT>(ix, a, num_sms, st, mid)
-                          : launch_sp<16, false, NT>(ix, a, num_sms, st, mid);
+            return direct ? launch_sp<16, true, NT>(ix, a, num_sms, st, mid, fin)
+                          : launch_sp<16, false, NT>(ix, a, num_sms, st, mid, fin);
     }
 }
 
 cudaError_t launch_scan_persistent(const DevIndex& ix, const ScanArgs& a, int num_sms, int threads, cudaStream_t st,
-                                   cudaEvent_t mid) {
+                                   cudaEvent_t mid, bool finalize) {
     if (a.nq <= 0) return cudaSuccess;
     if (!scan_persistent_supported(ix, a)) return cudaErrorNotSupported;
-    return threads == 1024 ? launch_sp_nt<1024>(ix, a, num_sms, st, mid) : launch_sp_nt<512>(ix, a, num_sms, st, mid);
+    if ((a.flags & SCAN_KEYS_ONLY) && (!a.tau_out || finalize)) return cudaErrorInvalidValue;
+    return threads == 1024 ? launch_sp_nt<1024>(ix, a, num_sms, st, mid, finalize)
+                           : launch_sp_nt<512>(ix, a, num_sms, st, mid, finalize);
 }
 
 }  // namespace gbivf

@@ -15,6 +15,7 @@ Errors raise :class:`GbivfError` (the reference exits the process instead).
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 
 import numpy as np
 
@@ -87,6 +88,7 @@ class GpuIndex:
         b = _c(base, np.float32)
         check(self.lib.gbivf_index_set_base(self.h, _p(b), b.shape[0], b.shape[1]))
         self.base_rows = b.shape[0]
+        self.base_key = None
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -113,6 +115,13 @@ class GpuIndex:
             return _lib.GBIVF_MIXED_SCAN_AUTO
         return _lib.GBIVF_MIXED_SCAN if mixed_scan else 0
 
+    @staticmethod
+    def _order_flag(scan_order):
+        """scan_order: None (the engine's choice), "lists" (list by list) or "queries" (query by query)."""
+        if scan_order is None:
+            return 0
+        return {"lists": _lib.GBIVF_LIST_SCAN, "queries": _lib.GBIVF_QUERY_SCAN}[scan_order]
+
     def scan_form(self):
         """(tuned, mixed): the scan form mixed_scan="auto" resolves to on this index."""
         t, m = C.c_int(), C.c_int()
@@ -120,7 +129,7 @@ class GpuIndex:
         return bool(t.value), bool(m.value)
 
     def search(self, queries, k, w, kl=None, rerank=False, direct=False, out=None, mixed_coarse=False,
-               mixed_scan=False, refine=False):
+               mixed_scan=False, refine=False, scan_order=None):
         """ivfpq_search: (ids nq x k int32, dis nq x k float32). ``out`` may
         pass preallocated (ids, dis) host arrays (e.g. pinned memory)."""
         q = _c(queries, np.float32)
@@ -136,42 +145,65 @@ class GpuIndex:
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
+        flags |= self._order_flag(scan_order)
         check(self.lib.gbivf_ivfpq_search(self.h, _p(q), nq, k, kl if kl is not None else k, w, flags,
                                           _p(ids), _p(dis)))
         return ids, dis
 
     def search_device(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
-                      stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False, refine=False):
+                      stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False, refine=False,
+                      scan_order=None):
         """Device-pointer search (pointers as ints), enqueued on stream_ptr."""
         flags = (GBIVF_RERANK if rerank else 0) | (GBIVF_PROFILE if profile else 0)
         flags |= _lib.GBIVF_MIXED_COARSE if mixed_coarse else 0
         flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
+        flags |= self._order_flag(scan_order)
         check(self.lib.gbivf_ivfpq_search_device(self.h, C.c_void_p(d_queries_ptr), nq, k,
                                                  kl if kl is not None else k, w, flags, C.c_void_p(d_ids_ptr),
                                                  C.c_void_p(d_dis_ptr), C.c_void_p(stream_ptr)))
 
-    def search_batched(self, queries, w_per_q, k_per_q, mixed_coarse=False, mixed_scan=False):
+    def search_batched(self, queries, w_per_q, k_per_q, mixed_coarse=False, mixed_scan=False, out=None,
+                       scan_order=None):
         """Uneven batch: per-query nprobe and k. Returns (ids, dis, offsets):
-        query q's results are ids[offsets[q]:offsets[q+1]]."""
+        query q's results are ids[offsets[q]:offsets[q+1]]. ``out`` may pass preallocated
+        (ids, dis) host arrays of sum(k_per_q) entries (e.g. pinned memory)."""
         q = _c(queries, np.float32)
         wq = _c(w_per_q, np.int32)
         kq = _c(k_per_q, np.int32)
         off = np.zeros(len(kq) + 1, np.int64)
         np.cumsum(kq, out=off[1:])
-        ids = np.empty(int(off[-1]), np.int32)
-        dis = np.empty(int(off[-1]), np.float32)
+        if out is None:
+            ids = np.empty(int(off[-1]), np.int32)
+            dis = np.empty(int(off[-1]), np.float32)
+        else:
+            ids, dis = out
+            assert ids.shape == (int(off[-1]),) and ids.dtype == np.int32 and ids.flags.c_contiguous
+            assert dis.shape == (int(off[-1]),) and dis.dtype == np.float32 and dis.flags.c_contiguous
         flags = (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0) | self._scan_flag(mixed_scan)
+        flags |= self._order_flag(scan_order)
         check(self.lib.gbivf_search_batched(self.h, _p(q), q.shape[0], _p(wq), _p(kq), flags, _p(ids), _p(dis)))
         return ids, dis, off
 
+    def search_batched_device(self, d_queries_ptr, nq, d_w_ptr, d_k_ptr, d_off_ptr, max_w, max_k, d_ids_ptr,
+                              d_dis_ptr, stream_ptr=0, profile=False, mixed_coarse=False, mixed_scan=False,
+                              scan_order=None):
+        """Uneven batch on device buffers (pointers as ints), enqueued on stream_ptr."""
+        flags = (GBIVF_PROFILE if profile else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
+        flags |= self._scan_flag(mixed_scan) | self._order_flag(scan_order)
+        check(self.lib.gbivf_search_batched_device(self.h, C.c_void_p(d_queries_ptr), nq, C.c_void_p(d_w_ptr),
+                                                   C.c_void_p(d_k_ptr), C.c_void_p(d_off_ptr), max_w, max_k, flags,
+                                                   C.c_void_p(d_ids_ptr), C.c_void_p(d_dis_ptr),
+                                                   C.c_void_p(stream_ptr)))
+
     def capture_graph(self, d_queries_ptr, nq, k, w, d_ids_ptr, d_dis_ptr, kl=None, rerank=False,
                       mixed_coarse=False, d_w_ptr=0, d_k_ptr=0, d_off_ptr=0, stream_ptr=0, mixed_scan=False,
-                      refine=False):
+                      refine=False, scan_order=None):
         """Capture a device-buffer search as a CUDA graph (see gbivf_graph_capture)."""
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
         flags |= self._scan_flag(mixed_scan)
         flags |= _lib.GBIVF_RERANK_REFINE if refine else 0
+        flags |= self._order_flag(scan_order)
         g = C.c_void_p()
         check(self.lib.gbivf_graph_capture(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
                                            flags, C.c_void_p(d_ids_ptr), C.c_void_p(d_dis_ptr), C.c_void_p(d_w_ptr),
@@ -201,6 +233,16 @@ class GpuIndex:
         a, b, c = C.c_float(), C.c_float(), C.c_float()
         check(self.lib.gbivf_last_stages_ms(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def last_scan_parts(self):
+        """(parts_ms, counters) of the last profiled search's scan stage (gbivf_last_scan_parts):
+        planning, first pass, grouping, list-centric scan, selection, overflow pass, finalize; and
+        pairs scanned list by list, work items, overflowed queries, 1 if it ran list by list."""
+        p = (C.c_float * 7)()
+        c = (C.c_int64 * 4)()
+        check(self.lib.gbivf_last_scan_parts(self.h, p, c))
+        names = ["plan", "first_pass", "grouping", "list_scan", "select", "overflow_pass", "finalize"]
+        return dict(zip(names, list(p))), dict(zip(["pairs", "items", "overflowed", "list_scan"], list(c)))
 
     def coarse_assign(self, queries, w, mixed=False, stats=False, full=False):
         """knn_full over the coarse centroids: (coaidx, coadis) nq x w. With
@@ -238,6 +280,12 @@ class SearchGraph:
     def launch(self, stream_ptr=0):
         check(self.lib.gbivf_graph_launch(self.h, C.c_void_p(stream_ptr)))
 
+    def kernel_count(self) -> int:
+        """Kernel launches per replay."""
+        n = C.c_int()
+        check(self.lib.gbivf_graph_kernel_count(self.h, C.byref(n)))
+        return n.value
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.gbivf_graph_destroy(self.h)
@@ -274,11 +322,20 @@ class GpuPQ(GpuIndex):
         return dis, ids
 
 
+def _content_key(a: np.ndarray) -> tuple:
+    """Shape and a digest of the bytes: tells one base from another even when the caller refills
+    the same array in place (the reference rewrites vectors in place, ivf_assign.cpp:15)."""
+    a = np.ascontiguousarray(a, np.float32)
+    return a.shape, hashlib.blake2b(memoryview(a).cast("B"), digest_size=16).digest()
+
+
 def ivfpq_search(index: GpuIndex, vquery, vbase, k, kl, w):
     """The reference signature's semantics: always re-ranks kl -> k against
-    vbase (uploaded once per index). Returns (ids, dis)."""
-    if getattr(index, "base_rows", 0) != len(vbase):
+    vbase (uploaded again whenever its contents change). Returns (ids, dis)."""
+    key = _content_key(vbase)
+    if getattr(index, "base_key", None) != key:
         index.set_base(vbase)
+        index.base_key = key
     return index.search(vquery, k, w, kl=kl, rerank=True)
 
 

@@ -108,6 +108,33 @@ class IVFPQData:
         np.savez_compressed(path, coa=self.coa, pq=self.pq, list_off=self.list_off, ids=self.ids, codes=self.codes,
                             **extra)
 
+    def save_dir(self, path: str) -> None:
+        """Uncompressed arrays, one .npy file each, under directory `path` (fast for GB-sized
+        indexes; written to a temporary name first and renamed, so a reader never sees half)."""
+        import os
+
+        tmp = f"{path}.tmp{os.getpid()}"
+        os.makedirs(tmp, exist_ok=True)
+        arrays = dict(coa=self.coa, pq=self.pq, list_off=self.list_off, ids=self.ids, codes=self.codes)
+        if self.pq2 is not None:
+            arrays.update(pq2=self.pq2, codes2=self.codes2)
+        for k, v in arrays.items():
+            np.save(os.path.join(tmp, f"{k}.npy"), v)
+        os.replace(tmp, path)
+
+    @staticmethod
+    def load_dir(path: str) -> "IVFPQData":
+        import os
+
+        def get(k):
+            f = os.path.join(path, f"{k}.npy")
+            return np.load(f) if os.path.exists(f) else None
+
+        out = IVFPQData(coa=get("coa"), pq=get("pq"), list_off=get("list_off").astype(np.int64), ids=get("ids"),
+                        codes=get("codes"), pq2=get("pq2"), codes2=get("codes2"))
+        out.validate()
+        return out
+
     @staticmethod
     def load(path: str) -> "IVFPQData":
         z = np.load(path)

@@ -1,0 +1,82 @@
+"""The large workloads against the CPU oracle, on GPU-built indexes.
+
+* the 10M workload at full size (10,000,000 x 128 base, 4,096-component
+  mixture, C = 65,536 lists, m = 8, w = 32, k = 100);
+* the 100M workload's shape at 1/25 scale (4,000,000 base, Zipf(1.1)
+  component sizes, C = 16,384 lists, m = 16, per-query nprobe log-uniform in
+  1..256 and k from {1, 10, 100, 1000}).
+
+The plain form must return the oracle's ids and distance bits on every
+sampled query (both keyed by (distance, position in the probe order)); the
+sample holds the queries with the largest k and nprobe. The precision form
+returns exact distances for every id it returns (bit-identical to the plain
+form's), and its ids are the plain form's on (at least) 99% of the queries."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _build(ncomp, zipf, nbase, ntrain, C, m, nq, seed=0, iters=6):
+    import torch
+
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
+    from mestrado_gb300.synth import Mixture
+
+    gm = GpuMixture(Mixture(d=128, ncomp=ncomp, seed=seed, zipf=zipf))
+    base = gm.generate(nbase, stream_id=1)
+    train = gm.generate(ntrain, stream_id=2)
+    ix = build_index_gpu(base, train, C, m, niter=iters, seed=seed)
+    q = gm.generate(nq, stream_id=3).cpu().numpy()
+    del base, train
+    torch.cuda.empty_cache()
+    return ix, q
+
+
+def _sample(wq, kq, n):
+    """The n queries with the most work (largest k, then nprobe) and a spread of the rest."""
+    order = np.lexsort((-wq, -kq))
+    heavy = order[: n // 2]
+    rest = np.setdiff1d(np.arange(len(wq)), heavy)[:: max(1, (len(wq) - n // 2) // (n - n // 2))][: n - n // 2]
+    return np.sort(np.concatenate([heavy, rest]))
+
+
+def _check(ix, q, wq, kq, nsample):
+    import oracle
+    from mestrado_gb300.engine import GpuIndex
+
+    gi = GpuIndex(ix)
+    p_ids, p_dis, off = gi.search_batched(q, wq, kq)
+    m_ids, m_dis, _ = gi.search_batched(q, wq, kq, mixed_coarse=True, mixed_scan=True)
+    gi.close()
+    sel = _sample(wq, kq, nsample)
+    o_ids, o_dis, o_off = oracle.search_batched(ix, q[sel], wq[sel], kq[sel], nthreads=16)
+    for j, i in enumerate(sel):
+        np.testing.assert_array_equal(p_ids[off[i]:off[i + 1]], o_ids[o_off[j]:o_off[j + 1]], err_msg=f"query {i}")
+        np.testing.assert_array_equal(p_dis[off[i]:off[i + 1]].view(np.uint32),
+                                      o_dis[o_off[j]:o_off[j + 1]].view(np.uint32), err_msg=f"query {i}")
+    same = 0
+    for i in range(len(q)):
+        a, b = p_ids[off[i]:off[i + 1]], m_ids[off[i]:off[i + 1]]
+        same += int(np.array_equal(a, b))
+        pd = dict(zip(a.tolist(), p_dis[off[i]:off[i + 1]].view(np.uint32).tolist()))
+        for x, y in zip(b.tolist(), m_dis[off[i]:off[i + 1]].view(np.uint32).tolist()):
+            assert x < 0 or x not in pd or pd[x] == y, f"query {i}: id {x} distance differs between the forms"
+    assert same >= 0.99 * len(q), (same, len(q))
+    return sel
+
+
+def test_10m_workload_plain_matches_oracle_on_sample():
+    ix, q = _build(ncomp=4096, zipf=None, nbase=10_000_000, ntrain=1_000_000, C=65536, m=8, nq=1000, iters=8)
+    wq = np.full(len(q), 32, np.int32)
+    kq = np.full(len(q), 100, np.int32)
+    _check(ix, q, wq, kq, 64)
+
+
+def test_100m_shape_uneven_plain_matches_oracle_on_sample():
+    ix, q = _build(ncomp=16384, zipf=1.1, nbase=4_000_000, ntrain=400_000, C=16384, m=16, nq=2048)
+    rng = np.random.default_rng(17)
+    wq = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(257), len(q)))), 1, 256).astype(np.int32)
+    kq = rng.choice([1, 10, 100, 1000], len(q)).astype(np.int32)
+    sel = _check(ix, q, wq, kq, 96)
+    assert kq[sel].max() == 1000 and wq[sel].max() >= 200

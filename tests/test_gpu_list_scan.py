@@ -1,0 +1,176 @@
+"""The list-centric scan (GBIVF_LIST_SCAN): the batch's (query, probe) pairs
+grouped by list, G queries per work item, a first pass over each query's
+nearest probes for its threshold, emission of the keys below it, exact
+selection, and the overflow pass. Its results must be the per-query scan's
+bit for bit (ids and distances), and the oracle's (keyed tie rule), in both
+scan forms, on the golden cases, on uneven batches with k up to 1000, on a
+GPU-built index with a few thousand queries, through the overflow pass (a
+tiny emission buffer) and inside a CUDA graph."""
+import numpy as np
+import pytest
+
+import oracle
+from tests import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b, what):
+    np.testing.assert_array_equal(a[0], b[0], err_msg=f"{what}: ids")
+    np.testing.assert_array_equal(a[1].view(np.uint32), b[1].view(np.uint32), err_msg=f"{what}: distances")
+
+
+@pytest.mark.parametrize("name", ["cfg1", "m16"])
+def test_golden_cases_list_equals_query_and_oracle(name):
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load(name)
+    gi = GpuIndex(g.ix, base=g.base)
+    w = g.meta["w"]
+    for k, kl, rerank in ((100, 100, True), (10, 60, True), (1, 1, False), (37, 37, False)):
+        res = {}
+        for mixed in (False, True):
+            res[mixed] = gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=mixed, scan_order="lists")
+            qry = gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=mixed, scan_order="queries")
+            _same(res[mixed], qry, f"{name} k={k} kl={kl} rerank={rerank} mixed={mixed}")
+        o = oracle.ivfpq_search(g.ix, g.queries, k=k, kl=kl, w=w, base=g.base if rerank else None, rerank=rerank,
+                                ties=oracle.TIES_KEYED)
+        _same(res[False], o, f"{name} k={k} vs oracle")
+    gi.close()
+
+
+def test_list_scan_needs_d128():
+    from mestrado_gb300._lib import GbivfError
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load("small")  # d = 32
+    gi = GpuIndex(g.ix)
+    with pytest.raises(GbivfError):
+        gi.search(g.queries, 5, 3, scan_order="lists")
+    gi.close()
+
+
+@pytest.mark.parametrize("name", ["cfg1", "m16"])
+def test_uneven_batches(name):
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load(name)
+    rng = np.random.default_rng(9)
+    nq = len(g.queries)
+    wq = rng.integers(1, g.ix.coarsek + 1, nq).astype(np.int32)
+    kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
+    gi = GpuIndex(g.ix)
+    res = {}
+    for mixed in (False, True):
+        res[mixed] = gi.search_batched(g.queries, wq, kq, mixed_coarse=mixed, mixed_scan=mixed, scan_order="lists")
+        qry = gi.search_batched(g.queries, wq, kq, mixed_coarse=mixed, mixed_scan=mixed, scan_order="queries")
+        _same(res[mixed][:2], qry[:2], f"{name} mixed={mixed}")
+    o_ids, o_dis, _ = oracle.search_batched(g.ix, g.queries, wq, kq)
+    _same(res[False][:2], (o_ids, o_dis), f"{name} vs oracle")
+    gi.close()
+
+
+def _gpu_index(nbase=600_000, C=2048, m=16, nq=4096, seed=3):
+    import torch
+
+    from mestrado_gb300.gpu_build import GpuMixture, build_index_gpu
+    from mestrado_gb300.synth import Mixture
+
+    gm = GpuMixture(Mixture(d=128, ncomp=C, seed=seed, zipf=1.1))
+    base = gm.generate(nbase, stream_id=1)
+    train = gm.generate(100_000, stream_id=2)
+    ix = build_index_gpu(base, train, C, m, niter=4, seed=seed)
+    q = gm.generate(nq, stream_id=3).cpu().numpy()
+    del base, train
+    torch.cuda.empty_cache()
+    return ix, q
+
+
+@pytest.fixture(scope="module")
+def built():
+    return _gpu_index()
+
+
+def test_gpu_built_index_list_equals_query(built):
+    from mestrado_gb300.engine import GpuIndex
+
+    ix, q = built
+    rng = np.random.default_rng(4)
+    wq = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(129), len(q)))), 1, 128).astype(np.int32)
+    kq = rng.choice([1, 10, 100, 1000], len(q)).astype(np.int32)
+    gi = GpuIndex(ix)
+    for mixed in (False, True):
+        lst = gi.search_batched(q, wq, kq, mixed_coarse=mixed, mixed_scan=mixed, scan_order="lists")
+        qry = gi.search_batched(q, wq, kq, mixed_coarse=mixed, mixed_scan=mixed, scan_order="queries")
+        _same(lst[:2], qry[:2], f"mixed={mixed}")
+    # and a uniform batch with re-rank-free k = 100, w = 32
+    lst = gi.search(q, 100, 32, scan_order="lists")
+    qry = gi.search(q, 100, 32, scan_order="queries")
+    _same(lst, qry, "uniform")
+    gi.close()
+
+
+def test_overflow_pass(built, monkeypatch):
+    """With an emission buffer of 16 keys most queries overflow and are scanned again query by
+    query; the results do not change."""
+    import torch
+
+    from mestrado_gb300.engine import GpuIndex
+
+    ix, q = built
+    q = q[:1536]
+    rng = np.random.default_rng(6)
+    wq = rng.integers(1, 65, len(q)).astype(np.int32)
+    kq = rng.choice([10, 100, 1000], len(q)).astype(np.int32)
+    ref = GpuIndex(ix)
+    expect = {m: ref.search_batched(q, wq, kq, mixed_scan=m, scan_order="queries") for m in (False, True)}
+    ref.close()
+    monkeypatch.setenv("GBIVF_LIST_SCAN_CAP", "16")
+    gi = GpuIndex(ix)
+    off = expect[False][2]
+    d_q = torch.from_numpy(q).cuda()
+    d_w, d_k = torch.from_numpy(wq).cuda(), torch.from_numpy(kq).cuda()
+    d_off = torch.from_numpy(off[:-1].copy()).cuda()
+    d_ids = torch.empty(int(off[-1]), dtype=torch.int32, device="cuda")
+    d_dis = torch.empty(int(off[-1]), dtype=torch.float32, device="cuda")
+    for mixed in (False, True):
+        gi.search_batched_device(d_q.data_ptr(), len(q), d_w.data_ptr(), d_k.data_ptr(), d_off.data_ptr(),
+                                 int(wq.max()), int(kq.max()), d_ids.data_ptr(), d_dis.data_ptr(), profile=True,
+                                 mixed_scan=mixed, scan_order="lists")
+        torch.cuda.synchronize()
+        parts, counters = gi.last_scan_parts()
+        assert counters["list_scan"] == 1 and counters["overflowed"] > len(q) // 4, counters
+        _same((d_ids.cpu().numpy(), d_dis.cpu().numpy()), expect[mixed][:2], f"overflow mixed={mixed}")
+    gi.close()
+
+
+def test_graph_replay_list_scan(built):
+    import torch
+
+    from mestrado_gb300.engine import GpuIndex
+
+    ix, q = built
+    nq = 2048
+    rng = np.random.default_rng(8)
+    wq = rng.integers(1, 97, nq).astype(np.int32)
+    kq = rng.choice([1, 10, 100, 1000], nq).astype(np.int32)
+    gi = GpuIndex(ix)
+    expect = gi.search_batched(q[:nq], wq, kq, mixed_coarse=True, mixed_scan=True, scan_order="queries")
+    off = expect[2]
+    d_q = torch.from_numpy(q[:nq].copy()).cuda()
+    d_w, d_k = torch.from_numpy(wq).cuda(), torch.from_numpy(kq).cuda()
+    d_off = torch.from_numpy(off[:-1].copy()).cuda()
+    d_ids = torch.empty(int(off[-1]), dtype=torch.int32, device="cuda")
+    d_dis = torch.empty(int(off[-1]), dtype=torch.float32, device="cuda")
+    s = torch.cuda.Stream()
+    graph = gi.capture_graph(d_q.data_ptr(), nq, int(kq.max()), int(wq.max()), d_ids.data_ptr(), d_dis.data_ptr(),
+                             mixed_coarse=True, mixed_scan=True, d_w_ptr=d_w.data_ptr(), d_k_ptr=d_k.data_ptr(),
+                             d_off_ptr=d_off.data_ptr(), stream_ptr=s.cuda_stream, scan_order="lists")
+    assert graph.kernel_count() > 5
+    for _ in range(2):
+        d_ids.fill_(-5)
+        graph.launch(s.cuda_stream)
+        s.synchronize()
+        _same((d_ids.cpu().numpy(), d_dis.cpu().numpy()), expect[:2], "graph replay")
+    graph.close()
+    gi.close()

@@ -53,10 +53,51 @@ def test_noalloc_matches_allocating_coarse_assign():
         np.testing.assert_array_equal(d_idx.cpu().numpy(), ref_idx)
         np.testing.assert_array_equal(d_dis.cpu().numpy().view(np.uint32), ref_dis.view(np.uint32))
 
-    # a batch beyond the scratch is refused with a clear error
-    too_many = _lib.load().gbivf_coarse_assign_noalloc(gi.h, C.c_void_p(d_q.data_ptr()), 5000, 4,
-                                                        C.c_void_p(d_idx.data_ptr()),
-                                                        C.c_void_p(d_dis.data_ptr()), C.c_void_p(stream))
+    # the largest batch that fits (4,088 queries at coarsek = 1024: 16 MiB exactly) runs; one more
+    # query is refused with a clear error naming that limit
+    limit = 4088
+    q = np.rint(np.clip(rng.normal(60, 30, (limit + 1, 128)), 0, 255)).astype(np.float32)
+    d_q = torch.from_numpy(q).cuda()
+    d_idx = torch.empty((limit + 1, 4), dtype=torch.int32, device="cuda")
+    d_dis = torch.empty((limit + 1, 4), dtype=torch.float32, device="cuda")
+    rc = lib.gbivf_coarse_assign_noalloc(gi.h, C.c_void_p(d_q.data_ptr()), limit, 4, C.c_void_p(d_idx.data_ptr()),
+                                         C.c_void_p(d_dis.data_ptr()), C.c_void_p(stream))
+    _lib.check(rc)
+    torch.cuda.synchronize()
+    ref_idx, _ = gi.coarse_assign(q[:limit], 4)
+    np.testing.assert_array_equal(d_idx[:limit].cpu().numpy(), ref_idx)
+    too_many = lib.gbivf_coarse_assign_noalloc(gi.h, C.c_void_p(d_q.data_ptr()), limit + 1, 4,
+                                               C.c_void_p(d_idx.data_ptr()), C.c_void_p(d_dis.data_ptr()),
+                                               C.c_void_p(stream))
     assert too_many == 4
-    assert b"scratch" in lib.gbivf_last_error()
+    msg = lib.gbivf_last_error()
+    assert b"scratch" in msg and b"at most 4088 queries" in msg, msg
+    gi.close()
+
+
+def test_noalloc_matches_filtered_coarse_stage():
+    """At coarsek >= 16,384 the allocating call takes the large-C filter (a sampled bound, then
+    exact re-checks); the allocation-free call always selects over the full distance block. Both
+    are exact, so they agree bit for bit."""
+    import torch
+
+    from mestrado_gb300 import _lib
+    from mestrado_gb300.engine import GpuIndex
+
+    lib = _lib.load()
+    ix, rng = _index(seed=5, C_=16384)
+    gi = GpuIndex(ix)
+    stream = torch.cuda.current_stream().cuda_stream
+    for nq, w in ((240, 32), (97, 64)):
+        q = np.rint(np.clip(rng.normal(60, 30, (nq, 128)), 0, 255)).astype(np.float32)
+        d_q = torch.from_numpy(q).cuda()
+        d_idx = torch.full((nq, w), -7, dtype=torch.int32, device="cuda")
+        d_dis = torch.full((nq, w), -7.0, dtype=torch.float32, device="cuda")
+        _lib.check(lib.gbivf_coarse_assign_noalloc(gi.h, C.c_void_p(d_q.data_ptr()), nq, w,
+                                                   C.c_void_p(d_idx.data_ptr()), C.c_void_p(d_dis.data_ptr()),
+                                                   C.c_void_p(stream)))
+        torch.cuda.synchronize()
+        ref_idx, ref_dis = gi.coarse_assign(q, w)
+        np.testing.assert_array_equal(d_idx.cpu().numpy(), ref_idx)
+        np.testing.assert_array_equal(d_dis.cpu().numpy().view(np.uint32), ref_dis.view(np.uint32))
     gi.close()
