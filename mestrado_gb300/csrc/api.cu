@@ -355,8 +355,9 @@ int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
         return r;
     };
     const size_t o_w0 = take(4 * nq), o_pcnt = take(4 * C), o_pbeg = take(4 * (C + 1)), o_fill = take(4 * C),
-                 o_gbeg = take(4 * (C + 1)), o_pairs = take(16 * P), o_groups = take(16 * P), o_cnt = take(4 * 8),
+                 o_gbeg = take(4 * (C + 1)), o_pairs = take(16 * P), o_groups = take(16 * 9 * P), o_cnt = take(4 * 8),
                  o_keys = take(8 * nq * a.cand_stride), o_cntA = take(4 * nq), o_tau = take(8 * nq),
+                 o_tau0 = take(8 * nq), o_hist = take(4 * nq * (int64_t)LC_HIST_BUCKETS),
                  o_ebuf = take(8 * nq * (int64_t)w.ecap), o_ecnt = take(4 * nq), o_ovf = take(4 * nq);
     CK(ix->lc_ws.ensure(off));
     unsigned char* b = ix->lc_ws.as<unsigned char>();
@@ -373,6 +374,8 @@ int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
     w.keysA = reinterpret_cast<unsigned long long*>(b + o_keys);
     w.cntA = reinterpret_cast<int*>(b + o_cntA);
     w.tau = reinterpret_cast<unsigned long long*>(b + o_tau);
+    w.tau0 = reinterpret_cast<unsigned long long*>(b + o_tau0);
+    w.hist = reinterpret_cast<unsigned int*>(b + o_hist);
     w.ebuf = reinterpret_cast<unsigned long long*>(b + o_ebuf);
     w.ecnt = reinterpret_cast<int*>(b + o_ecnt);
     w.ovf = reinterpret_cast<int32_t*>(b + o_ovf);

@@ -122,11 +122,13 @@ struct ListScanWork {
     int* fill = nullptr;      // C: fill cursors
     int* gbeg = nullptr;      // C + 1: first group of each list
     int4* pairs = nullptr;    // max_pairs: (query, probe, position of the probe's first row, 0), by list
-    int4* groups = nullptr;   // max_pairs: (list, first pair, pairs, 0)
+    int4* groups = nullptr;   // max_pairs x (1 + G): work-item descriptors (scan_lists.cu)
     int* counters = nullptr;  // [0] groups, [1] work counter, [2] overflowed queries
     unsigned long long* keysA = nullptr;  // nq x cand_stride: the first pass's best keys ...
     int* cntA = nullptr;                  // ... and their count
-    unsigned long long* tau = nullptr;    // nq: the first pass's k-th key (KEY_MAX: fewer rows)
+    unsigned long long* tau0 = nullptr;   // nq: the first pass's k-th key (KEY_MAX: fewer rows)
+    unsigned long long* tau = nullptr;    // nq: the current bound, lowered during the scan
+    unsigned int* hist = nullptr;         // nq x LC_HIST_BUCKETS: emitted keys by distance below tau0
     unsigned long long* ebuf = nullptr;   // nq x ecap: keys below tau from the list-centric pass ...
     int* ecnt = nullptr;                  // ... and their count (may exceed ecap: overflow)
     int ecap = 0;
@@ -134,8 +136,9 @@ struct ListScanWork {
     int* err = nullptr;       // device error flag (a bounded wait ran out)
     int* queue_a = nullptr;   // work counters of the first pass and of the overflow pass
     int* queue_b = nullptr;
-    int beta = 2;             // the first pass scans each query's nearest probes until beta * k_sel rows
+    int beta = 1;             // the first pass scans each query's nearest probes until beta * k_sel rows
 };
+constexpr int LC_HIST_BUCKETS = 256;
 bool list_scan_supported(const DevIndex& ix, const ScanArgs& a);
 int list_scan_ecap(const ScanArgs& a);
 // The list-centric search pipeline up to the finalize hand-off (a.cand_*): planning, first pass,

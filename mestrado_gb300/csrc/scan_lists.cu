@@ -18,18 +18,28 @@
 //
 // Top-k without per-query state in the CTA: a first pass (the query-centric
 // kernel, SCAN_KEYS_ONLY) scans each query's nearest probes until it holds
-// 2 k_sel rows and hands off its k_sel best keys and the k_sel-th key tau_q.
+// k_sel rows and hands off its k_sel best keys and the k_sel-th key tau_q.
 // Every key of the exact top-k_sel over all probes is <= tau_q, so the
 // list-centric pass appends only keys below tau_q, to a per-query buffer in
-// global memory. The select kernel takes the k_sel smallest of both sets
-// (exact radix select) and writes the finalize kernel's hand-off; a query
-// whose buffer overflowed is scanned again by the query-centric kernel.
-// Results are identical to the query-centric path's.
+// global memory. That first bound is loose (in 128 dimensions the nearest
+// lists are hardly closer than the 200th), so the bound moves: the first
+// pass's keys and every emitted key are counted in a per-query histogram of
+// their distance below the first bound (256 buckets of 2^15 float ulps, about
+// 0.4 % each), and each time a query's emissions pass a multiple of k_sel / 4
+// the emitting warp finds
+// the lowest bucket edge with k_sel counted keys below it and lowers tau_q to
+// it (atomicMin). Any such edge bounds the k_sel-th key from above, so every
+// work item read afterwards filters harder and none loses a true candidate.
+// The select kernel takes the k_sel smallest of both sets (exact radix
+// select) and writes the finalize kernel's hand-off; a query whose buffer
+// still overflowed is scanned again by the query-centric kernel. Results are
+// identical to the query-centric path's.
 #include <cuda_fp16.h>
 
 #include "block_topk.cuh"
 #include "exact_round.cuh"
 #include "f32x2.cuh"
+#include "rot_codes.cuh"
 #include "scan_common.cuh"
 #include "tc_common.cuh"
 
@@ -38,6 +48,8 @@ namespace gbivf {
 constexpr int LC_NT = 512;        // threads of the list-centric scan (one CTA per SM)
 constexpr int LC_TILE = 16384;    // bytes of code rows per staged tile
 constexpr int LC_SEL_NT = 256;    // threads of the select kernel (one CTA per query)
+constexpr int LC_SEL_STAGE = 3072;  // keys of a query's pool the select kernel stages in shared memory
+constexpr int LC_HIST_SHIFT = 15;   // histogram bucket width: 2^15 float ulps below the first bound
 
 template <bool MIXED>
 struct LcShape {
@@ -127,10 +139,26 @@ __global__ void __launch_bounds__(1024) lc_prefix_kernel(int C, ListScanWork w) 
 
 // One warp per query: the position of each probe's first row in the query's candidate order (the
 // prefix of list lengths over all its probes) and a pair record per probe the first pass left.
-__global__ void lc_fill_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
-    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+// Also starts the query's bound at the first pass's, and its histogram with the first pass's keys.
+__global__ void __launch_bounds__(256) lc_fill_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
+    __shared__ unsigned int s_h[8][LC_HIST_BUCKETS];
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     if (q >= a.nq) return;
     const int wq = query_w(a, q), p = w.w0[q];
+    const u64 t0k = w.tau0[q];
+    if (lane == 0) w.tau[q] = t0k;
+    for (int i = lane; i < LC_HIST_BUCKETS; i += 32) s_h[wp][i] = 0u;
+    __syncwarp();
+    if (t0k != KEY_MAX) {
+        const uint32_t t0 = (uint32_t)(t0k >> 32);
+        const int na = w.cntA[q];
+        for (int i = lane; i < na; i += 32) {
+            const uint32_t below = t0 - (uint32_t)(w.keysA[(int64_t)q * a.cand_stride + i] >> 32);
+            atomicAdd(&s_h[wp][min(LC_HIST_BUCKETS - 1, (int)(below >> LC_HIST_SHIFT))], 1u);
+        }
+    }
+    __syncwarp();
+    for (int i = lane; i < LC_HIST_BUCKETS; i += 32) w.hist[(int64_t)q * LC_HIST_BUCKETS + i] = s_h[wp][i];
     uint32_t carry = 0;
     for (int j0 = 0; j0 < wq; j0 += 32) {
         const int j = j0 + lane;
@@ -150,13 +178,27 @@ __global__ void lc_fill_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
     }
 }
 
-// One thread per list: its groups of up to G pairs.
+// One thread per list: the descriptors of its work items, each up to G of its pairs. A descriptor is
+// 1 + G 16-byte words: (list, pairs, 0, 0), then per slot (query, position of the probe's first row,
+// k_sel, float key of the first pass's bound) -- everything the scan needs but the current bound.
 template <int G>
-__global__ void lc_groups_kernel(int C, ListScanWork w) {
+__global__ void lc_groups_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= C) return;
+    if (l >= ix.C) return;
     const int pb = w.pbeg[l], n = w.pbeg[l + 1] - pb, g0 = w.gbeg[l];
-    for (int g = 0; g * G < n; g++) w.groups[g0 + g] = make_int4(l, pb + g * G, min(G, n - g * G), 0);
+    for (int g = 0; g * G < n; g++) {
+        int4* d = w.groups + (int64_t)(g0 + g) * (1 + G);
+        const int np = min(G, n - g * G);
+        d[0] = make_int4(l, np, 0, 0);
+        for (int i = 0; i < G; i++) {
+            if (i < np) {
+                const int4 pr = w.pairs[pb + g * G + i];
+                d[1 + i] = make_int4(pr.x, pr.z, lc_ksel(a, pr.x), (int)(uint32_t)(w.tau0[pr.x] >> 32));
+            } else {
+                d[1 + i] = make_int4(-1, 0, 1, 0);
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -171,6 +213,49 @@ __device__ __forceinline__ float lc_add_h(float acc, uint32_t word, int hi) {
     return acc;
 }
 
+__device__ __forceinline__ void lc_cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void lc_cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void lc_cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+
+// One warp: the lowest bucket edge of query q's histogram with at least k_sel emitted keys at or below
+// it; tau_q drops to that edge. Bucket i counts keys whose float key lies 2^15 i .. 2^15 (i + 1) - 1
+// ulps below the first bound t0 (the last bucket everything lower), so the keys at or below edge j,
+// t0 - 2^15 j, are exactly those in buckets j and up.
+__device__ __forceinline__ void lc_lower_bound(const ListScanWork& w, int q, uint32_t t0, int ksel, int lane) {
+    constexpr int PER = LC_HIST_BUCKETS / 32;
+    const unsigned int* hq = w.hist + (int64_t)q * LC_HIST_BUCKETS;
+    uint32_t c[PER], sum = 0;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        c[i] = __ldcg(hq + lane * PER + i);
+        sum += c[i];
+    }
+    // keys in the buckets of higher lanes (suffix sum over the warp, exclusive)
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_down_sync(0xffffffffu, incl, o);
+        if (lane + o < 32) incl += v;
+    }
+    uint32_t above = incl - sum;
+    int best = -1;  // the largest bucket index j with sum over buckets >= j of at least ksel
+#pragma unroll
+    for (int i = PER - 1; i >= 0; i--) {
+        above += c[i];
+        if (best < 0 && above >= (uint32_t)ksel) best = lane * PER + i;
+    }
+    const unsigned cand = __ballot_sync(0xffffffffu, best >= 0);
+    if (!cand) return;
+    const int src = 31 - __clz(cand);  // the highest lane that found one holds the largest j
+    const int j = __shfl_sync(0xffffffffu, best, src);
+    const uint32_t edge = t0 - ((uint32_t)j << LC_HIST_SHIFT);
+    if (lane == 0 && j > 0 && edge > 0x80000000u) atomicMin(w.tau + q, ((u64)edge << 32) | 0xffffffffull);
+}
+
 template <int M, bool MIXED>
 __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs a, ListScanWork w) {
     constexpr int NT = LC_NT, D = 128, KS = 256, DS = D / M;
@@ -181,22 +266,29 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
     constexpr int TILE_GROUPS = LC_TILE / 16;
     constexpr int TILE_ROWS = LC_TILE / M;
     constexpr int UG = TILE_GROUPS / NT;  // 16-byte groups per thread per tile
-    static_assert(E % 2 == 0 && E * TPS == KS && UG * NT == TILE_GROUPS, "shape");
-    static_assert(G * GR <= 32, "pass bits of a group fit one word");
+    constexpr int RS = UG * GR;           // rows per thread per tile
+    constexpr int RB = 2;                 // rows looked up together (independent chains)
+    static_assert(E % 2 == 0 && E * TPS == KS && UG * NT == TILE_GROUPS && RS % RB == 0, "shape");
+    static_assert(G * RB <= 32, "pass bits of a batch fit one word");
 
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint4* stage = reinterpret_cast<uint4*>(smem);                       // 2 x LC_TILE
-    unsigned char* tab = smem + 2 * LC_TILE;                             // M x 256 x 16 bytes
-    float* rr = reinterpret_cast<float*>(tab + M * KS * 16);             // G x D residuals
-    float* rn = rr + G * D;                                              // G x M sub-norms
-    __shared__ int s_q[G];
-    __shared__ uint32_t s_pos0[G];
-    __shared__ u64 s_tau[G];
-    __shared__ int s_next, s_abort;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint4* stage = reinterpret_cast<uint4*>(smem);              // 2 x LC_TILE of code rows
+    unsigned char* tab = smem + 2 * LC_TILE;                    // M x 256 x 16 bytes
+    float* xs = reinterpret_cast<float*>(tab + M * KS * 16);    // [2][G][D]: the queries of this item and the next
+    float* ys = xs + 2 * G * D;                                 // [2][D]: their list centroids
+    float* rr = ys + 2 * D;                                     // [G][D]: this item's residuals
+    int4* desc = reinterpret_cast<int4*>(rr + G * D);           // [2][1 + G]: this item's descriptor and the next
+    __shared__ __align__(16) u64 s_taup[2 * G];  // per slot the 16-byte pair of bounds holding its query's
+    __shared__ u64 s_tau[G];                       // per slot its query's bound
+    __shared__ int s_abort;
     __shared__ __align__(8) uint64_t bar[2];
 
     const int tid = threadIdx.x, lane = tid & 31;
-    const int my_s = tid / TPS, my_cl = tid % TPS;
+    // The exact form's table is sub-quantizer-major ([s][c][g]): a warp owns one sub-quantizer and its
+    // lanes consecutive centroids. The precision form's is sub-quantizer-minor ([c][s][g], slot c m + s,
+    // see rot_codes.cuh): its lanes take consecutive sub-quantizers of one centroid. Either way a warp's
+    // 16-byte table stores are contiguous.
+    const int my_s = MIXED ? tid % M : tid / TPS, my_cl = MIXED ? tid / M : tid % TPS;
 
     // this thread's slice of the codebook: entries (my_s, my_cl + TPS * i), i < E
     constexpr int EP = MIXED ? 1 : E, EM = MIXED ? E / 2 : 1;
@@ -238,52 +330,70 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_next = atomicAdd(&w.counters[1], 1);
         s_abort = 0;
     }
-    const int ngroups = w.counters[0];
+    // Work items are taken in a fixed order, this CTA's being blockIdx.x, + gridDim.x, ..., so the
+    // next item is known ahead: warp 0 copies its descriptor (cp.async) while this item's tables are
+    // built and its query vectors and list centroid while this item is scanned.
+    const int nitems = w.counters[0], istep = gridDim.x;
+    auto fetch_desc = [&](int bb, int it) {
+        if (lane <= G) lc_cp_async16(desc + bb * (1 + G) + lane, w.groups + (int64_t)it * (1 + G) + lane);
+        lc_cp_async_commit();
+    };
+    // every thread: at most one 16-byte chunk of the query vectors or of the list centroid
+    auto fetch_vectors = [&](int bb) {
+        const int4 hd = desc[bb * (1 + G)];
+        const int nc = hd.y * (D / 4);
+        if (tid < nc) {
+            const int g = tid / (D / 4), x4 = tid % (D / 4);
+            lc_cp_async16(xs + (bb * G + g) * D + 4 * x4, a.queries + (int64_t)desc[bb * (1 + G) + 1 + g].x * D + 4 * x4);
+        } else if (tid < nc + D / 4) {
+            lc_cp_async16(ys + bb * D + 4 * (tid - nc), ix.coa + (int64_t)hd.x * D + 4 * (tid - nc));
+        }
+        lc_cp_async_commit();
+    };
+    if ((int)blockIdx.x < nitems) {
+        if (tid < 32) {
+            fetch_desc(0, blockIdx.x);
+            lc_cp_async_wait_all();
+        }
+        __syncthreads();
+        fetch_vectors(0);
+    }
     uint32_t phase = 0;   // bit s: the parity the next wait on stage s expects
     uint32_t tc = 0;      // tiles consumed so far: tile tc uses stage tc & 1
     bool armed[2] = {false, false};
+    bool pre = false;     // thread 0: this item's first tile was copied during the previous item
+    int b = 0;            // this item's descriptor buffer
 
-    for (;;) {
-        __syncthreads();  // the previous item's table and stages are no longer read
-        const int gi = s_next;
-        if (gi >= ngroups || s_abort) break;
-        const int4 gd = w.groups[gi];
-        const int l = gd.x, pb = gd.y, np = gd.z;
+    for (int it = blockIdx.x;; it += istep, b ^= 1) {
+        lc_cp_async_wait_all();  // this item's vectors (each thread its own chunk)
+        __syncthreads();  // the previous item's table and stages are no longer read; this item's data is in
+        if (it >= nitems || s_abort) break;
+        const int4 hd = desc[b * (1 + G)];
+        const int l = hd.x, np = hd.y;
+        const int4* slot = desc + b * (1 + G) + 1;  // per query: (query, first-row position, k_sel, t0)
         const int len = __ldg(ix.list_len + l);
         const uint8_t* codes = ix.codes + __ldg(ix.list_beg + l) * (int64_t)M;
         const int nbytes = (len * M + 15) & ~15;  // the code array is padded to whole 16-byte groups
         const int ntiles = (nbytes + LC_TILE - 1) / LC_TILE;
-        if (tid < G) {
-            if (tid < np) {
-                const int4 pr = w.pairs[pb + tid];
-                s_q[tid] = pr.x;
-                s_pos0[tid] = (uint32_t)pr.z;
-                s_tau[tid] = w.tau[pr.x];
-            } else {
-                s_q[tid] = -1;
-                s_pos0[tid] = 0u;
-                s_tau[tid] = 0ull;  // nothing passes
-            }
-        }
-        if (tid == 0) {
-            s_next = atomicAdd(&w.counters[1], 1);
+        if (tid == 0 && !pre) {  // (normally copied already, during the previous item's last tile)
             const int st = tc & 1;
             mbar_expect_tx(&bar[st], (uint32_t)min(nbytes, LC_TILE));
             bulk_load(stage + st * TILE_GROUPS, codes, (uint32_t)min(nbytes, LC_TILE), &bar[st]);
             armed[st] = true;
         }
-        __syncthreads();
-        // residuals r_g = x_q - y_l (bsxfunMINUS, ivf_search.cpp:155-172)
-        for (int e = tid; e < G * D; e += NT) {
-            const int g = e / D, x = e % D;
-            rr[e] = g < np ? __fsub_rn(__ldg(a.queries + (int64_t)s_q[g] * D + x), __ldg(ix.coa + (int64_t)l * D + x))
-                           : 0.0f;
+        pre = false;
+        if (tid < 32) {
+            // the queries' current bounds (the 16-byte pair holding each, from L2: other SMs lower them)
+            // and the next item's descriptor
+            if (lane < np) lc_cp_async16(s_taup + 2 * lane, w.tau + (slot[lane].x & ~1));
+            if (it + istep < nitems) fetch_desc(b ^ 1, it + istep);
+            else lc_cp_async_commit();
         }
-        __syncthreads();
-        for (int e = tid; e < np * M; e += NT) rn[e] = norm_f_seq(rr + e * DS, DS);
+        // residuals r = x_q - y_l (bsxfunMINUS, ivf_search.cpp:155-172)
+        for (int e = tid; e < G * D; e += NT)
+            rr[e] = e / D < np ? __fsub_rn(xs[b * G * D + e], ys[b * D + (e % D)]) : 0.0f;
         __syncthreads();
         // the G interleaved tables from the register codebook
         if constexpr (MIXED) {
@@ -292,17 +402,20 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
 #pragma unroll
             for (int g = 0; g < G; g++) {
                 if (g < np) {
-                    f2_t rs2[DS];
+                    float rs[DS];
                     const float4* r4 = reinterpret_cast<const float4*>(rr + g * D + my_s * DS);
 #pragma unroll
                     for (int v4 = 0; v4 < DS / 4; v4++) {
                         const float4 x = r4[v4];
-                        rs2[4 * v4] = f2_pack(x.x, x.x);
-                        rs2[4 * v4 + 1] = f2_pack(x.y, x.y);
-                        rs2[4 * v4 + 2] = f2_pack(x.z, x.z);
-                        rs2[4 * v4 + 3] = f2_pack(x.w, x.w);
+                        rs[4 * v4] = x.x;
+                        rs[4 * v4 + 1] = x.y;
+                        rs[4 * v4 + 2] = x.z;
+                        rs[4 * v4 + 3] = x.w;
                     }
-                    const float f4 = 0.25f * rn[g * M + my_s];
+                    f2_t rs2[DS];
+#pragma unroll
+                    for (int t = 0; t < DS; t++) rs2[t] = f2_pack(rs[t], rs[t]);
+                    const float f4 = 0.25f * norm_f_seq(rs, DS);
                     const f2_t f42 = f2_pack(f4, f4), mh2 = f2_pack(-0.5f, -0.5f);
 #pragma unroll
                     for (int p = 0; p < EM; p++) {
@@ -329,31 +442,36 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
                     const uint4 v = make_uint4(__byte_perm(hw[0][p], hw[1][p], sel), __byte_perm(hw[2][p], hw[3][p], sel),
                                                __byte_perm(hw[4][p], hw[5][p], sel), __byte_perm(hw[6][p], hw[7][p], sel));
                     const int c = my_cl + TPS * (2 * p + h);
-                    *reinterpret_cast<uint4*>(tab + ((my_s * KS + c) << 4)) = v;
+                    *reinterpret_cast<uint4*>(tab + ((c * M + my_s) << 4)) = v;
                 }
             }
         } else {
             // the reference's entry: -2 <r_s, c> + (float)(||c||^2 + ||r_s||^2) (nn.c:113-150), the dot
-            // product's products as fma(r, c, -0) (one rounding, never fused with the add)
-            float out[G][E];
+            // product's products as fma(r, c, -0) (one rounding, never fused with the add); entry pairs
+            // outermost, so that the G queries' values of an entry are stored as one 16-byte word
             const f2_t m2 = f2_pack(-2.0f, -2.0f), nz2 = f2_pack(a.neg_zero, a.neg_zero);
+            float fq[G];
 #pragma unroll
-            for (int g = 0; g < G; g++) {
-                if (g < np) {
-                    float rs[DS];
-                    const float4* r4 = reinterpret_cast<const float4*>(rr + g * D + my_s * DS);
+            for (int g = 0; g < G; g++) fq[g] = g < np ? norm_f_seq(rr + g * D + my_s * DS, DS) : 0.0f;
 #pragma unroll
-                    for (int v4 = 0; v4 < DS / 4; v4++) {
-                        const float4 x = r4[v4];
-                        rs[4 * v4] = x.x;
-                        rs[4 * v4 + 1] = x.y;
-                        rs[4 * v4 + 2] = x.z;
-                        rs[4 * v4 + 3] = x.w;
-                    }
-                    const float f = rn[g * M + my_s];
-                    const f2_t f2 = f2_pack(f, f);
+            for (int i = 0; i < E; i += 2) {
+                float o0[G], o1[G];
+                const int e = my_s * KS + my_cl + TPS * i;
 #pragma unroll
-                    for (int i = 0; i < E; i += 2) {
+                for (int g = 0; g < G; g++) {
+                    if (g < np) {
+                        float rs[DS];
+                        const float4* r4 = reinterpret_cast<const float4*>(rr + g * D + my_s * DS);
+#pragma unroll
+                        for (int v4 = 0; v4 < DS / 4; v4++) {
+                            const float4 x = r4[v4];
+                            rs[4 * v4] = x.x;
+                            rs[4 * v4 + 1] = x.y;
+                            rs[4 * v4 + 2] = x.z;
+                            rs[4 * v4 + 3] = x.w;
+                        }
+                        const float f = fq[g];
+                        const f2_t f2 = f2_pack(f, f);
                         f2_t d2 = f2_pack(0.0f, 0.0f);
 #pragma unroll
                         for (int t = 0; t < DS; t++)
@@ -368,33 +486,25 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
                         float Sa, Sb, ta, tb;
                         f2_unpack(S2, Sa, Sb);
                         f2_unpack(t2, ta, tb);
-                        const int e = my_s * KS + my_cl + TPS * i;
                         const f2_t c02 = f2_pack(add_norms_finish(ix.pq_norm + e, Sa, ta, f),
                                                  add_norms_finish(ix.pq_norm + e + TPS, Sb, tb, f));
-                        f2_unpack(f2_add(f2_mul(m2, f2_pack(d0, d1)), c02), out[g][i], out[g][i + 1]);
+                        f2_unpack(f2_add(f2_mul(m2, f2_pack(d0, d1)), c02), o0[g], o1[g]);
+                    } else {
+                        o0[g] = o1[g] = 0.0f;
                     }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < E; i++) out[g][i] = 0.0f;
                 }
-            }
-#pragma unroll
-            for (int i = 0; i < E; i++) {
                 const int c = my_cl + TPS * i;
-                *reinterpret_cast<float4*>(tab + ((my_s * KS + c) << 4)) =
-                    make_float4(out[0][i], out[1][i], out[2][i], out[3][i]);
+                *reinterpret_cast<float4*>(tab + ((my_s * KS + c) << 4)) = make_float4(o0[0], o0[1], o0[2], o0[3]);
+                *reinterpret_cast<float4*>(tab + ((my_s * KS + c + TPS) << 4)) = make_float4(o1[0], o1[1], o1[2], o1[3]);
             }
         }
-        int qg[G];
-        uint32_t pos0[G];
-        u64 tau[G];
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            qg[g] = s_q[g];
-            pos0[g] = s_pos0[g];
-            tau[g] = s_tau[g];
+        if (tid < 32) {
+            lc_cp_async_wait_all();  // the bounds (each lane waits for its own copy) and the next descriptor
+            if (lane < G) s_tau[lane] = lane < np ? s_taup[2 * lane + (slot[lane].x & 1)] : 0ull;  // 0: nothing passes
         }
-        __syncthreads();  // tables written
+        __syncthreads();  // tables written; bounds in
+        if (it + istep < nitems) fetch_vectors(b ^ 1);  // they arrive during this item's scan
+        const u64* tau = s_tau;
 
         for (int t = 0; t < ntiles; t++, tc++) {
             const int st = tc & 1;
@@ -408,85 +518,158 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
             }
             phase ^= 1u << st;
             armed[st] = false;
-            if (tid == 0 && t + 1 < ntiles) {
-                const int nb = min(LC_TILE, nbytes - (t + 1) * LC_TILE);
-                mbar_expect_tx(&bar[st ^ 1], (uint32_t)nb);
-                bulk_load(stage + (st ^ 1) * TILE_GROUPS, codes + (int64_t)(t + 1) * LC_TILE, (uint32_t)nb,
-                          &bar[st ^ 1]);
-                armed[st ^ 1] = true;
+            if (tid == 0) {
+                // the tile after this one: this item's next, or the next item's first (its descriptor
+                // has been in since the table barrier)
+                const uint8_t* src = nullptr;
+                int nb = 0;
+                if (t + 1 < ntiles) {
+                    src = codes + (int64_t)(t + 1) * LC_TILE;
+                    nb = min(LC_TILE, nbytes - (t + 1) * LC_TILE);
+                } else if (it + istep < nitems) {
+                    const int nl = desc[(b ^ 1) * (1 + G)].x;
+                    src = ix.codes + __ldg(ix.list_beg + nl) * (int64_t)M;
+                    nb = min(LC_TILE, (__ldg(ix.list_len + nl) * M + 15) & ~15);
+                    pre = true;
+                }
+                if (src) {
+                    mbar_expect_tx(&bar[st ^ 1], (uint32_t)nb);
+                    bulk_load(stage + (st ^ 1) * TILE_GROUPS, src, (uint32_t)nb, &bar[st ^ 1]);
+                    armed[st ^ 1] = true;
+                }
             }
             const uint4* sg = stage + st * TILE_GROUPS;
             const int row0 = t * TILE_ROWS;
             const int ngt = min(TILE_GROUPS, (min(TILE_ROWS, len - row0) * M + 15) / 16);
+            uint4 cg[UG];
 #pragma unroll
             for (int u = 0; u < UG; u++) {
                 const int gl = u * NT + tid;
-                if (u * NT + (tid & ~31) >= ngt) break;  // warp-uniform
-                const uint4 c = gl < ngt ? sg[gl] : make_uint4(0, 0, 0, 0);
-                const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
-                float acc[GR][G];
-                uint32_t pass = 0;
+                cg[u] = gl < ngt ? sg[gl] : make_uint4(0, 0, 0, 0);
+            }
 #pragma unroll
-                for (int r = 0; r < GR; r++) {
-                    const int row = row0 + gl * GR + r;
-                    if constexpr (MIXED) {
-                        float s8[G];
+            for (int r0 = 0; r0 < RS; r0 += RB) {
+                if ((r0 / GR) * NT + (tid & ~31) >= ngt) break;  // warp-uniform: no rows left for this warp
+                // rows r0 .. r0 + RB - 1 of this thread: row slot r is row r % GR of group u = r / GR
+                float acc[RB][G];
+                int rowv[RB];
 #pragma unroll
-                        for (int g = 0; g < G; g++) s8[g] = 0.0f;
+                for (int rb = 0; rb < RB; rb++) {
+                    const int r = r0 + rb;
+                    rowv[rb] = row0 + ((r / GR) * NT + tid) * GR + r % GR;
+                }
+                if constexpr (MIXED) {
+                    // row-rotated order (rot_codes.cuh): the lanes of a quarter-warp, consecutive rows, read
+                    // different sub-quantizers, i.e. different bank quads of the [c][s] table
+                    float s8[RB][G];
+                    uint4 rc[RB];
 #pragma unroll
-                        for (int s = 0; s < M; s++) {
-                            const uint32_t b = lc_byte(cw[(r * M + s) >> 2], (r * M + s) & 3);
-                            const uint4 v = *reinterpret_cast<const uint4*>(tab + ((s * KS + b) << 4));
+                    for (int rb = 0; rb < RB; rb++) {
+#pragma unroll
+                        for (int g = 0; g < G; g++) s8[rb][g] = 0.0f;
+                        const int r = r0 + rb, rr = r % GR;
+                        const uint4 c = cg[r / GR];
+                        const int rot = row_rot<M>(rowv[rb]);
+                        if constexpr (M == 16) {
+                            rc[rb] = rot_bytes(c, rot);
+                        } else if constexpr (M == 8) {
+                            const uint2 v = rot_bytes(rr == 0 ? make_uint2(c.x, c.y) : make_uint2(c.z, c.w), rot);
+                            rc[rb] = make_uint4(v.x, v.y, 0u, 0u);
+                        } else {
+                            rc[rb] = make_uint4(rot_bytes(row_word(c, rr), rot), 0u, 0u, 0u);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < M; k++) {
+#pragma unroll
+                        for (int rb = 0; rb < RB; rb++) {
+                            const int sk = (k + row_rot<M>(rowv[rb])) & (M - 1);
+                            const uint32_t bidx = lc_byte(row_word(rc[rb], k >> 2), k & 3);
+                            const uint4 v = *reinterpret_cast<const uint4*>(tab + ((bidx * M + sk) << 4));
                             const uint32_t vw[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                            for (int g = 0; g < G; g++) s8[g] = lc_add_h(s8[g], vw[g >> 1], g & 1);
+                            for (int g = 0; g < G; g++) s8[rb][g] = lc_add_h(s8[rb][g], vw[g >> 1], g & 1);
                         }
-#pragma unroll
-                        for (int g = 0; g < G; g++) acc[r][g] = s8[g] * 4.0f;
-                    } else {
-                        f2_t a01 = f2_pack(0.0f, 0.0f), a23 = f2_pack(0.0f, 0.0f);
-#pragma unroll
-                        for (int s = 0; s < M; s++) {
-                            const uint32_t b = lc_byte(cw[(r * M + s) >> 2], (r * M + s) & 3);
-                            const float4 v = *reinterpret_cast<const float4*>(tab + ((s * KS + b) << 4));
-                            a01 = f2_add(a01, f2_pack(v.x, v.y));
-                            a23 = f2_add(a23, f2_pack(v.z, v.w));
-                        }
-                        f2_unpack(a01, acc[r][0], acc[r][1]);
-                        f2_unpack(a23, acc[r][2], acc[r][3]);
                     }
-                    const bool valid = gl < ngt && row < len;
+#pragma unroll
+                    for (int rb = 0; rb < RB; rb++)
+#pragma unroll
+                        for (int g = 0; g < G; g++) acc[rb][g] = s8[rb][g] * 4.0f;
+                } else {
+                    f2_t a01[RB], a23[RB];
+#pragma unroll
+                    for (int rb = 0; rb < RB; rb++) a01[rb] = a23[rb] = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                    for (int s = 0; s < M; s++) {
+#pragma unroll
+                        for (int rb = 0; rb < RB; rb++) {
+                            const int r = r0 + rb, u = r / GR, rr = r % GR;
+                            const uint4 c = cg[u];
+                            const uint32_t cw = (rr * M + s) >> 2 == 0 ? c.x
+                                              : (rr * M + s) >> 2 == 1 ? c.y
+                                              : (rr * M + s) >> 2 == 2 ? c.z : c.w;
+                            const uint32_t bidx = lc_byte(cw, (rr * M + s) & 3);
+                            const float4 v = *reinterpret_cast<const float4*>(tab + ((s * KS + bidx) << 4));
+                            a01[rb] = f2_add(a01[rb], f2_pack(v.x, v.y));
+                            a23[rb] = f2_add(a23[rb], f2_pack(v.z, v.w));
+                        }
+                    }
+#pragma unroll
+                    for (int rb = 0; rb < RB; rb++) {
+                        f2_unpack(a01[rb], acc[rb][0], acc[rb][1]);
+                        f2_unpack(a23[rb], acc[rb][2], acc[rb][3]);
+                    }
+                }
+                uint32_t pass = 0;
+#pragma unroll
+                for (int rb = 0; rb < RB; rb++) {
+                    const int gl = ((r0 + rb) / GR) * NT + tid;
+                    const bool valid = gl < ngt && rowv[rb] < len;
 #pragma unroll
                     for (int g = 0; g < G; g++) {
-                        const u64 key = make_key(acc[r][g], pos0[g] + (uint32_t)row);
-                        if (valid && key < tau[g]) pass |= 1u << (g * GR + r);
+                        const u64 key = make_key(acc[rb][g], (uint32_t)slot[g].y + (uint32_t)rowv[rb]);
+                        if (valid && key < tau[g]) pass |= 1u << (g * RB + rb);
                     }
                 }
                 if (__any_sync(0xffffffffu, pass != 0)) {
                     const unsigned lt = (1u << lane) - 1u;
+                    // each query's survivors in this batch; lane g reserves query g's slots, all queries in
+                    // one round trip to L2
+                    int mytot = 0;
 #pragma unroll
                     for (int g = 0; g < G; g++) {
-                        unsigned msk[GR];
                         int tot = 0;
 #pragma unroll
-                        for (int r = 0; r < GR; r++) {
-                            msk[r] = __ballot_sync(0xffffffffu, (pass >> (g * GR + r)) & 1u);
-                            tot += __popc(msk[r]);
-                        }
-                        if (tot == 0) continue;  // warp-uniform
-                        int base = 0;
-                        if (lane == 0) base = atomicAdd(&w.ecnt[qg[g]], tot);
-                        base = __shfl_sync(0xffffffffu, base, 0);
-                        u64* out = w.ebuf + (int64_t)qg[g] * w.ecap;
+                        for (int rb = 0; rb < RB; rb++) tot += __popc(__ballot_sync(0xffffffffu, (pass >> (g * RB + rb)) & 1u));
+                        if (lane == g) mytot = tot;
+                    }
+                    int mybase = 0;
+                    if (lane < G && mytot > 0) mybase = atomicAdd(&w.ecnt[slot[lane].x], mytot);
 #pragma unroll
-                        for (int r = 0; r < GR; r++) {
-                            if ((pass >> (g * GR + r)) & 1u) {
-                                const int idx = base + __popc(msk[r] & lt);
-                                if (idx < w.ecap)
-                                    out[idx] = make_key(acc[r][g], pos0[g] + (uint32_t)(row0 + gl * GR + r));
+                    for (int g = 0; g < G; g++) {
+                        const int tot = __shfl_sync(0xffffffffu, mytot, g);
+                        if (tot == 0) continue;  // warp-uniform
+                        const int q = slot[g].x;
+                        int base = __shfl_sync(0xffffffffu, mybase, g);
+                        const int base0 = base;
+                        u64* out = w.ebuf + (int64_t)q * w.ecap;
+                        unsigned int* hq = w.hist + (int64_t)q * LC_HIST_BUCKETS;
+#pragma unroll
+                        for (int rb = 0; rb < RB; rb++) {
+                            const unsigned msk = __ballot_sync(0xffffffffu, (pass >> (g * RB + rb)) & 1u);
+                            if ((pass >> (g * RB + rb)) & 1u) {
+                                const int idx = base + __popc(msk & lt);
+                                const u64 key = make_key(acc[rb][g], (uint32_t)slot[g].y + (uint32_t)rowv[rb]);
+                                if (idx < w.ecap) out[idx] = key;
+                                const uint32_t below = (uint32_t)slot[g].w - (uint32_t)(key >> 32);
+                                atomicAdd(hq + min(LC_HIST_BUCKETS - 1, (int)(below >> LC_HIST_SHIFT)), 1u);
                             }
-                            base += __popc(msk[r]);
+                            base += __popc(msk);
                         }
+                        // past a multiple of k_sel / 4 emitted keys: a tighter bound from the histogram
+                        const int step = max(slot[g].z / 4, 32);
+                        if (base0 / step != (base0 + tot) / step)
+                            lc_lower_bound(w, q, (uint32_t)slot[g].w, slot[g].z, lane);
                     }
                 }
             }
@@ -513,16 +696,26 @@ __global__ void __launch_bounds__(LC_SEL_NT) lc_select_kernel(DevIndex ix, ScanA
         if (tid == 0) w.ovf[atomicAdd(&w.counters[2], 1)] = q;
         return;
     }
-    const int stride = a.cand_stride, wq = query_w(a, q);
-    u64* pool = reinterpret_cast<u64*>(smem);                            // na + ne keys
-    uint32_t* prefix = reinterpret_cast<uint32_t*>(pool + stride + w.ecap);  // wq + 1
-    int* plist = reinterpret_cast<int*>(prefix + a.w + 1);                // wq
+    const int stride = a.cand_stride, wq = query_w(a, q), n = na + ne;
+    u64* stage = reinterpret_cast<u64*>(smem);                                // LC_SEL_STAGE keys
+    uint32_t* prefix = reinterpret_cast<uint32_t*>(stage + LC_SEL_STAGE);     // wq + 1
+    int* plist = reinterpret_cast<int*>(prefix + a.w + 1);                    // wq
     unsigned char* work = reinterpret_cast<unsigned char*>(plist + a.w + 1);
     work = reinterpret_cast<unsigned char*>(((uintptr_t)work + 15) & ~(uintptr_t)15);
     __shared__ int s_cnt;
     TopKSmem s{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0, work};
-    for (int i = tid; i < na; i += LC_SEL_NT) pool[i] = w.keysA[(int64_t)q * stride + i];
-    for (int i = tid; i < ne; i += LC_SEL_NT) pool[na + i] = w.ebuf[(int64_t)q * w.ecap + i];
+    // the pool: staged in shared memory when it fits, else read in place (the radix passes then go
+    // to L2); a small stage keeps several CTAs per SM
+    const u64* A = w.keysA + (int64_t)q * stride;
+    const u64* B = w.ebuf + (int64_t)q * w.ecap;
+    int nA = na, nB = ne;
+    if (n <= LC_SEL_STAGE) {
+        for (int i = tid; i < na; i += LC_SEL_NT) stage[i] = A[i];
+        for (int i = tid; i < ne; i += LC_SEL_NT) stage[na + i] = B[i];
+        A = stage;
+        nA = n;
+        nB = 0;
+    }
     for (int j = tid; j < wq; j += LC_SEL_NT) {
         const int l = __ldg(a.probes + (int64_t)q * a.w + j);
         plist[j] = l;
@@ -549,14 +742,14 @@ __global__ void __launch_bounds__(LC_SEL_NT) lc_select_kernel(DevIndex ix, ScanA
         }
         if (lane == 0) prefix[wq] = carry;
     }
-    const int n = na + ne, K = min(lc_ksel(a, q), n);
+    const int K = min(lc_ksel(a, q), n);
     u64 T = KEY_MAX;
-    if (n > K && K > 0) T = block_kth(s, pool, n, pool, 0, K);  // the K-th smallest key
+    if (n > K && K > 0) T = block_kth(s, A, nA, B, nB, K);  // the K-th smallest key
     __syncthreads();
     const int64_t o0 = (int64_t)q * stride;
     for (int i0 = 0; i0 < n; i0 += LC_SEL_NT) {
         const int i = i0 + tid;
-        const u64 key = i < n ? pool[i] : KEY_MAX;
+        const u64 key = i < nA ? A[i] : (i < n ? B[i - nA] : KEY_MAX);
         const bool keep = i < n && key <= T && K > 0;
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (!m) continue;
@@ -594,7 +787,10 @@ bool list_scan_supported(const DevIndex& ix, const ScanArgs& a) {
     return scan_persistent_supported(ix, a) && !(a.flags & (SCAN_TABLE_DIRECT | SCAN_SRC_RESIDUAL | SCAN_OUT_PACKED));
 }
 
-int list_scan_ecap(const ScanArgs& a) { return 2 * scan_persistent_stride(a) + 2048; }
+// Keys a query may emit below its threshold. The first pass's k-th key ranks well beyond k over all
+// probes for large k (measured at the 100M workload: with 2 k + 2048 slots about one query in seven
+// overflowed), so the buffer holds 8 k + 2048; untouched slots cost nothing.
+int list_scan_ecap(const ScanArgs& a) { return 8 * scan_persistent_stride(a) + 2048; }
 
 template <int M, bool MIXED>
 static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListScanWork& w, int num_sms,
@@ -616,7 +812,7 @@ static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListSc
     pa.cand_cnt = w.cntA;
     pa.cand_id = nullptr;
     pa.cand_list = nullptr;
-    pa.tau_out = w.tau;
+    pa.tau_out = w.tau0;
     pa.queue = w.queue_a;
     if ((e = rec(0)) != cudaSuccess) return e;
     if ((e = launch_scan_persistent(ix, pa, num_sms, 512, st, nullptr, false)) != cudaSuccess) return e;
@@ -625,10 +821,11 @@ static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListSc
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     lc_fill_kernel<<<wblocks, 256, 0, st>>>(ix, a, w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    lc_groups_kernel<G><<<(C + 255) / 256, 256, 0, st>>>(C, w);
+    lc_groups_kernel<G><<<(C + 255) / 256, 256, 0, st>>>(ix, a, w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = rec(2)) != cudaSuccess) return e;
-    const size_t smem = 2 * LC_TILE + (size_t)M * 256 * 16 + sizeof(float) * (G * 128 + G * M);
+    const size_t smem = 2 * LC_TILE + (size_t)M * 256 * 16 + sizeof(float) * (3 * G * 128 + 2 * 128) +
+                        sizeof(int4) * 2 * (1 + G);
     auto kern = lc_scan_kernel<M, MIXED>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return e;
@@ -636,8 +833,7 @@ static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListSc
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = rec(3)) != cudaSuccess) return e;
     const bool rows_out = (a.flags & (SCAN_MIXED | SCAN_REFINE)) != 0;
-    const size_t ssm = sizeof(u64) * ((size_t)a.cand_stride + w.ecap) + sizeof(int) * (2 * (size_t)a.w + 2) + 16 +
-                       TOPK_WORK_BYTES;
+    const size_t ssm = sizeof(u64) * LC_SEL_STAGE + sizeof(int) * (2 * (size_t)a.w + 2) + 16 + TOPK_WORK_BYTES;
     void (*sel)(DevIndex, ScanArgs, ListScanWork) = rows_out ? lc_select_kernel<true> : lc_select_kernel<false>;
     if ((e = cudaFuncSetAttribute(sel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm)) != cudaSuccess)
         return e;
