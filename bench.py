@@ -698,6 +698,9 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
         clocks = ClockSampler(local_rank)
         clocks.start()
         barrier()
+        window = args.profile_steps and form == "mixed"
+        if window:  # the range an external profiler started with --profile-from-start off captures
+            torch.cuda.profiler.start()
         total = 0.0
         for i in range(args.steps):
             with torch.cuda.stream(stream):
@@ -708,6 +711,8 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
                 ev1.record(stream)
             ev1.synchronize()
             total += ev0.elapsed_time(ev1)
+        if window:
+            torch.cuda.profiler.stop()
         barrier()
         clk = clocks.stop()
         graph.close()
@@ -715,17 +720,21 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
         ids = d_ids.cpu().numpy()
         dis = d_dis.cpu().numpy()
         # stage split: the mean of three profiled (non-graph) searches
-        st = []
+        st, parts_l = [], []
         for _ in range(3):
             flush.fill_(1)
             gi.search_batched_device(queries.data_ptr(), nq, d_w.data_ptr(), d_k.data_ptr(), d_off.data_ptr(),
                                      max_w, max_k, d_ids.data_ptr(), d_dis.data_ptr(), stream_ptr=sp, profile=True,
                                      **fl)
             st.append(stage_split(gi))
+            parts_l.append(gi.last_scan_parts())
         stages = {k_: statistics.mean(s[k_] for s in st) for k_ in st[0]}
+        scan_parts = {k_: statistics.mean(p_[0][k_] for p_ in parts_l) for k_ in parts_l[0][0]}
+        scan_counters = parts_l[-1][1]
         rec = packed_recall(ids, off, kq, gt, sample) if sample else {}
         forms[form] = dict(qps=whole_job_rate(nq, args.steps, world, total / 1000.0), ms_per_step=total / args.steps,
-                           stages=stages, gpu_launches_per_step=kernels, clocks=clk, ids=ids, dis=dis, **rec,
+                           stages=stages, scan_parts_ms=scan_parts, scan_counters=scan_counters,
+                           gpu_launches_per_step=kernels, clocks=clk, ids=ids, dis=dis, **rec,
                            adc_distance_error_vs_fp64=adc_error_fp64(ix, q_host, (ids, dis), off, kq,
                                                                      min(sample or 100, 100)))
     pl, mx = forms["plain"], forms["mixed"]
@@ -743,7 +752,21 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
         par["largest_nprobe_in_sample"] = int(wq[:ns].max())
 
     peak, peak_kind = measured_peak_hbm()
-    achieved = scan_bytes / (mx["stages"]["scan_kernel"] / 1000.0) / 1e9
+    # The dominant kernel of the mixed step. Scanned list by list, it is the list-centric kernel, whose
+    # algorithmic bytes are the codes of the probes the first pass left to it (the engine's rule: each
+    # query's leading probes up to beta * k_sel rows go to the first pass); else the per-query scan kernel.
+    if mx["scan_counters"]["list_scan"]:
+        sel = np.minimum(kq.astype(np.int64) * 4, 4096)  # the precision form's k_sel
+        rows = np.where(probed >= 0, sizes[np.maximum(probed, 0)], 0)
+        csum = np.cumsum(rows, axis=1)
+        lead = (csum < sel[:, None]).sum(1) + 1  # leading probes holding beta * k_sel rows (beta = 1)
+        lead = np.minimum(lead, wq)
+        lc_bytes = int(np.where(np.arange(max_w)[None, :] >= lead[:, None], rows, 0).sum()) * m
+        kern_name, kern_ms, kern_bytes = "lc_scan_kernel (mixed form)", mx["scan_parts_ms"]["list_scan"], lc_bytes
+    else:
+        kern_name, kern_ms, kern_bytes = "ivf_scan_persistent_kernel (mixed form)", mx["stages"]["scan_kernel"], scan_bytes
+    achieved = kern_bytes / (kern_ms / 1000.0) / 1e9
+    stage_ms = mx["stages"]["scan_kernel"]  # the whole scan stage before finalize (all its kernels)
     rec = {
         "workload": large_workload(name, c),
         "forms": {f: {k_: v for k_, v in forms[f].items() if k_ not in ("ids", "dis", "clocks")} for f in forms},
@@ -752,10 +775,15 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
         "recall_sample_queries": sample,
         "mixed_vs_plain": plain_vs_mixed,
         "parity_plain_vs_oracle": par,
-        "roofline": {"bound": "hbm", "kernel": "ivf_scan_persistent_kernel (mixed form)", "achieved": achieved,
-                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "bytes_per_launch": scan_bytes, "bytes_unique_per_launch": unique_bytes,
-                     "traffic": profiled_traffic(f"ivf_scan_{name}")},
+        "roofline": {"bound": "hbm", "kernel": kern_name, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": achieved / peak, "bytes_per_launch": kern_bytes, "kernel_ms": kern_ms,
+                     "traffic": profiled_traffic(f"lc_scan_{name}"),
+                     "scan_stage": {"bytes_per_step": scan_bytes, "bytes_unique_per_step": unique_bytes,
+                                    "ms": stage_ms, "gbs": scan_bytes / (stage_ms / 1000.0) / 1e9,
+                                    "frac": scan_bytes / (stage_ms / 1000.0) / 1e9 / peak,
+                                    "what": "every kernel between the coarse stage and finalize (first pass, "
+                                            "grouping, list-centric scan, selection, overflow pass) on all "
+                                            "probed codes"}},
         "index_build_s": t_build,
         "clocks": mx["clocks"], "clocks_plain": pl["clocks"],
     }
@@ -1122,6 +1150,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--no-sub", action="store_true", help="headline: skip the drop-in and 10M sub-records")
+    ap.add_argument("--profile-steps", action="store_true",
+                    help="large workloads: mark the mixed form's timed steps for a profiler started with "
+                         "--profile-from-start off (numbers printed under a profiler are not measurements)")
     ap.add_argument("--stage", default="search", choices=["search", "coarse"],
                     help="large configurations: time the whole search, or the coarse stage alone")
     ap.add_argument("--nbase", type=int, default=None,

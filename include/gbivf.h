@@ -71,8 +71,9 @@ extern "C" {
                                    a scan of its nearest probes. Same results as the per-query scan.
                                    Not with GBIVF_TABLE_DIRECT or GBIVF_QUERY_SCAN */
 #define GBIVF_QUERY_SCAN 0x200u /* scan query by query (one CTA per query at a time). Without either
-                                   flag the engine picks: the list-centric scan for batches of at
-                                   least 1024 queries where it applies */
+                                   flag the engine picks: the autotuner's measured choice, else the
+                                   list-centric scan for batches of at least 1024 queries on an index
+                                   whose lists average at most 768 codes, where it applies */
 #define GBIVF_PROFILE 0x100u    /* record CUDA events around the coarse and scan stages */
 #define GBIVF_ERR_TIMEOUT 5     /* a bounded device-side wait ran out (the kernel stopped and reported it) */
 
@@ -183,11 +184,13 @@ int gbivf_graph_destroy(gbivf_graph *g);
 int gbivf_graph_kernel_count(const gbivf_graph *g, int *kernels);
 
 /* Autotuner: times the scan kernels that can serve this index and search
- * shape (persistent register-codebook kernel with 512 or 1024 threads, or the
- * general kernel) on a calibration batch of device queries, keeps the fastest
- * for later searches on this index and reports it in *choice (512, 1024, or
- * 0 for the general kernel); times_ms (3 entries, may be NULL) receives each
- * variant's scan time, -1 where it does not apply. When the environment
+ * shape (persistent register-codebook kernel with 512 or 1024 threads, the
+ * general kernel, or the list-centric pipeline) on a calibration batch of
+ * device queries, keeps the fastest for later searches on this index (the
+ * list-centric choice applies to batches of 1024 queries or more, as the
+ * engine's own rule does) and reports it in *choice (512, 1024, 0 for the
+ * general kernel, 1 for the list-centric pipeline); times_ms (4 entries, may
+ * be NULL) receives each variant's scan time, -1 where it does not apply. When the environment
  * variable GBIVF_TUNE_CACHE names a file, choices are read from and appended
  * to it, keyed by index shape, list-size histogram, GPU and search shape. */
 /* The scan form GBIVF_MIXED_SCAN_AUTO resolves to on this index: *tuned = 1 once gbivf_index_autotune

@@ -138,7 +138,12 @@ struct gbivf_index {
     ListScanWork lcw;
     cudaEvent_t lc_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     bool last_list_scan = false;      // the last profiled search scanned list by list
-    bool list_default = true;         // without GBIVF_LIST_SCAN / GBIVF_QUERY_SCAN: list by list for large batches
+    // without GBIVF_LIST_SCAN / GBIVF_QUERY_SCAN: 0 = the engine's rule (list by list for batches of at least
+    // LIST_MIN_QUERIES on an index whose lists average at most LIST_MAX_MEAN_LEN codes), 1 = list by list for
+    // large batches, 2 = query by query; list_pref: the autotuner's measured choice (-1: none)
+    int list_mode = 0;
+    int list_pref = -1;
+    double mean_len = 0.0;
     int lc_ecap = 0;                  // per-query emission capacity of the list-centric scan (0: the default)
     // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -268,8 +273,9 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     if (const char* v = getenv("GBIVF_LIST_SCAN_BETA")) ix->lcw.beta = std::max(1, atoi(v));
     if (const char* v = getenv("GBIVF_SCAN_KERNEL")) {
         ix->use_persistent = strcmp(v, "general") != 0;
-        ix->list_default = strcmp(v, "lists") == 0;
+        ix->list_mode = strcmp(v, "lists") == 0 ? 1 : 2;
     }
+    ix->mean_len = coarsek ? (double)n / coarsek : 0.0;
 
     DevIndex& dx = ix->dx;
     dx.d = d;
@@ -385,9 +391,21 @@ int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
 }
 
 // whether this search scans list by list (GBIVF_LIST_SCAN, or the engine's choice for large batches)
+// The engine's default scan order. Measured on one GB300: list by list wins where lists are short
+// against the per-query scan's per-probe cost (100M / 262,144 lists, ~380 codes: 26.6 vs 39.3 ms;
+// 10M / 65,536 lists, ~150 codes: 3.8 vs 4.4 ms) and loses on long lists that the per-query kernel
+// already amortises (1M / 1,024 lists, ~980 codes: 3.7 vs 2.9 ms).
+constexpr int LIST_MIN_QUERIES = 1024;
+constexpr double LIST_MAX_MEAN_LEN = 768.0;
+
 bool use_list_scan(const gbivf_index* ix, const ScanArgs& a, unsigned gflags) {
     if (gflags & GBIVF_QUERY_SCAN) return false;
-    const bool want = (gflags & GBIVF_LIST_SCAN) || (ix->list_default && a.nq >= 1024);
+    bool want = gflags & GBIVF_LIST_SCAN;
+    if (!want && a.nq >= LIST_MIN_QUERIES) {
+        if (ix->list_mode == 1) want = true;
+        else if (ix->list_mode == 0)
+            want = ix->list_pref >= 0 ? ix->list_pref == 1 : ix->mean_len <= LIST_MAX_MEAN_LEN;
+    }
     return want && list_scan_supported(ix->dx, a);
 }
 
@@ -1014,8 +1032,10 @@ namespace {
 struct ScanVariant {
     bool persistent;
     int threads;
+    bool lists;  // the list-centric pipeline
 };
-constexpr ScanVariant kVariants[3] = {{true, 512}, {true, 1024}, {false, 0}};
+constexpr ScanVariant kVariants[4] = {{true, 512, false}, {true, 1024, false}, {false, 0, false}, {true, 512, true}};
+constexpr int kVariantCode[4] = {512, 1024, 0, 1};  // *choice and the tuning cache's value
 
 std::string tune_key(gbivf_index* ix, int k, int w, unsigned flags) {
     // index shape, a coarse histogram of list sizes, the GPU, and the search shape
@@ -1154,8 +1174,9 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
     if (cached_th >= 0) {
         ix->use_persistent = cached_th != 0;
         ix->scan_threads = cached_th == 1024 ? 1024 : 512;
+        ix->list_pref = cached_th == 1 ? 1 : 0;
         if (choice) *choice = cached_th;
-        if (times_ms) times_ms[0] = times_ms[1] = times_ms[2] = -1.0f;
+        if (times_ms) times_ms[0] = times_ms[1] = times_ms[2] = times_ms[3] = -1.0f;
         if (!auto_form) return GBIVF_OK;
         if (cached_form >= 0) {
             ix->auto_tuned = true;
@@ -1187,7 +1208,7 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
         const int save_t = ix->scan_threads;
         float best = 1e30f;
         int best_i = -1;
-        for (int i = 0; i < 3; i++) {
+        for (int i = 0; i < 4; i++) {
             ix->use_persistent = kVariants[i].persistent;
             ix->scan_threads = kVariants[i].persistent ? kVariants[i].threads : save_t;
             float t = -1.0f;
@@ -1198,9 +1219,12 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
             probe.kl = kl;
             probe.flags = flags & GBIVF_RERANK ? SCAN_RERANK : 0;
             probe.queue = ix->w_queue.as<int>();
-            const bool applies = !kVariants[i].persistent || scan_persistent_supported(ix->dx, probe);
+            const bool applies = kVariants[i].lists ? list_scan_supported(ix->dx, probe)
+                                                    : !kVariants[i].persistent || scan_persistent_supported(ix->dx, probe);
             if (applies) {
-                rc = time_scan(flags, &t);
+                rc = time_scan((flags & ~(GBIVF_LIST_SCAN | GBIVF_QUERY_SCAN)) |
+                                   (kVariants[i].lists ? GBIVF_LIST_SCAN : GBIVF_QUERY_SCAN),
+                               &t);
                 if (rc) break;
                 if (t < best) {
                     best = t;
@@ -1217,7 +1241,8 @@ int gbivf_index_autotune(gbivf_index* ix, const float* d_queries, int nq, int k,
         }
         ix->use_persistent = kVariants[best_i].persistent;
         ix->scan_threads = kVariants[best_i].persistent ? kVariants[best_i].threads : save_t;
-        const int th = kVariants[best_i].persistent ? kVariants[best_i].threads : 0;
+        ix->list_pref = kVariants[best_i].lists ? 1 : 0;
+        const int th = kVariantCode[best_i];
         if (choice) *choice = th;
         if (cache)
             if (FILE* f = fopen(cache, "a")) {

@@ -217,7 +217,7 @@ class GpuIndex:
         flags = (GBIVF_RERANK if rerank else 0) | (_lib.GBIVF_MIXED_COARSE if mixed_coarse else 0)
         flags |= _lib.GBIVF_MIXED_SCAN_AUTO if scan_form else 0
         ch = C.c_int()
-        t = (C.c_float * 3)()
+        t = (C.c_float * 4)()
         check(self.lib.gbivf_index_autotune(self.h, C.c_void_p(d_queries_ptr), nq, k, kl if kl is not None else k, w,
                                             flags, C.byref(ch), t))
         return ch.value, list(t)

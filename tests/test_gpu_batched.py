@@ -110,11 +110,11 @@ def test_autotune_picks_a_kernel_and_keeps_results(tmp_path, monkeypatch):
     d_q = torch.from_numpy(g.queries.copy()).cuda()
     before = gi.search(g.queries, 100, 4)
     choice, times = gi.autotune(d_q.data_ptr(), len(g.queries), 100, 4)
-    assert choice in (0, 512, 1024)
+    assert choice in (0, 1, 512, 1024)  # 1: the list-centric pipeline
     assert all(t > 0 for t in times)
     after = gi.search(g.queries, 100, 4)
     np.testing.assert_array_equal(before[0], after[0])
     assert cache.read_text().strip().endswith(str(choice))
     choice2, times2 = gi.autotune(d_q.data_ptr(), len(g.queries), 100, 4)  # served from the cache file
-    assert choice2 == choice and times2 == [-1.0, -1.0, -1.0]
+    assert choice2 == choice and times2 == [-1.0, -1.0, -1.0, -1.0]
     gi.close()
