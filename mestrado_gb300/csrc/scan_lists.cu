@@ -100,40 +100,76 @@ __global__ void lc_plan_kernel(DevIndex ix, ScanArgs a, ListScanWork w, int beta
 
 // One block: exclusive prefix sums over the C lists of the pair counts (pbeg) and of the groups
 // of G pairs (gbeg); fill cursors start at pbeg; the totals go to pbeg[C], gbeg[C], counters[0].
+// The lists go by in chunks of 4 per thread (4,096 per pass): coalesced loads, a warp-shuffle scan,
+// the warps' totals scanned by warp 0, a running carry.
 template <int G>
 __global__ void __launch_bounds__(1024) lc_prefix_kernel(int C, ListScanWork w) {
-    __shared__ int s_p[1024], s_g[1024];
-    const int tid = threadIdx.x, per = (C + 1023) / 1024;
-    const int b = min(C, tid * per), e = min(C, b + per);
-    int sp = 0, sg = 0;
-    for (int l = b; l < e; l++) {
-        const int c = w.pcnt[l];
-        sp += c;
-        sg += (c + G - 1) / G;
-    }
-    s_p[tid] = sp;
-    s_g[tid] = sg;
+    __shared__ int s_wp[32], s_wg[32], s_carry[2];
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    if (tid == 0) s_carry[0] = s_carry[1] = 0;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
-        const int vp = tid >= o ? s_p[tid - o] : 0, vg = tid >= o ? s_g[tid - o] : 0;
+    for (int base = 0; base < C; base += 4096) {
+        const int i0 = base + 4 * tid;
+        int c[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) c[j] = i0 + j < C ? w.pcnt[i0 + j] : 0;
+        int tp = 0, tg = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            tp += c[j];
+            tg += (c[j] + G - 1) / G;
+        }
+        int ip = tp, ig = tg;  // inclusive scan over the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int vp = __shfl_up_sync(0xffffffffu, ip, o), vg = __shfl_up_sync(0xffffffffu, ig, o);
+            if (lane >= o) {
+                ip += vp;
+                ig += vg;
+            }
+        }
+        if (lane == 31) {
+            s_wp[wp] = ip;
+            s_wg[wp] = ig;
+        }
         __syncthreads();
-        s_p[tid] += vp;
-        s_g[tid] += vg;
+        if (wp == 0) {  // exclusive scan of the 32 warp totals
+            const int vp = s_wp[lane], vg = s_wg[lane];
+            int jp = vp, jg = vg;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int up = __shfl_up_sync(0xffffffffu, jp, o), ug = __shfl_up_sync(0xffffffffu, jg, o);
+                if (lane >= o) {
+                    jp += up;
+                    jg += ug;
+                }
+            }
+            s_wp[lane] = jp - vp;
+            s_wg[lane] = jg - vg;
+        }
+        __syncthreads();
+        int rp = s_carry[0] + s_wp[wp] + ip - tp, rg = s_carry[1] + s_wg[wp] + ig - tg;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (i0 + j < C) {
+                w.pbeg[i0 + j] = rp;
+                w.fill[i0 + j] = rp;
+                w.gbeg[i0 + j] = rg;
+            }
+            rp += c[j];
+            rg += (c[j] + G - 1) / G;
+        }
+        __syncthreads();  // every thread has read the carry and the warp offsets
+        if (tid == 1023) {
+            s_carry[0] = rp;
+            s_carry[1] = rg;
+        }
         __syncthreads();
     }
-    int rp = s_p[tid] - sp, rg = s_g[tid] - sg;
-    for (int l = b; l < e; l++) {
-        const int c = w.pcnt[l];
-        w.pbeg[l] = rp;
-        w.fill[l] = rp;
-        w.gbeg[l] = rg;
-        rp += c;
-        rg += (c + G - 1) / G;
-    }
-    if (tid == 1023) {
-        w.pbeg[C] = s_p[1023];
-        w.gbeg[C] = s_g[1023];
-        w.counters[0] = s_g[1023];
+    if (tid == 0) {
+        w.pbeg[C] = s_carry[0];
+        w.gbeg[C] = s_carry[1];
+        w.counters[0] = s_carry[1];
     }
 }
 
