@@ -728,13 +728,14 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
                                      **fl)
             st.append(stage_split(gi))
             parts_l.append(gi.last_scan_parts())
+        unproven = gi.last_unproven()  # precision form: queries not proven equal to the exact form
         stages = {k_: statistics.mean(s[k_] for s in st) for k_ in st[0]}
         scan_parts = {k_: statistics.mean(p_[0][k_] for p_ in parts_l) for k_ in parts_l[0][0]}
         scan_counters = parts_l[-1][1]
         rec = packed_recall(ids, off, kq, gt, sample) if sample else {}
         forms[form] = dict(qps=whole_job_rate(nq, args.steps, world, total / 1000.0), ms_per_step=total / args.steps,
                            stages=stages, scan_parts_ms=scan_parts, scan_counters=scan_counters,
-                           gpu_launches_per_step=kernels, clocks=clk, ids=ids, dis=dis, **rec,
+                           unproven_queries=unproven, gpu_launches_per_step=kernels, clocks=clk, ids=ids, dis=dis, **rec,
                            adc_distance_error_vs_fp64=adc_error_fp64(ix, q_host, (ids, dis), off, kq,
                                                                      min(sample or 100, 100)))
     pl, mx = forms["plain"], forms["mixed"]

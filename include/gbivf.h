@@ -47,10 +47,12 @@ extern "C" {
                                    the results are the same either way */
 #define GBIVF_MIXED_SCAN 0x10u  /* precision form of the scan (d = 128, ks = 256, m in {4, 8, 16}): PQ tables
                                    built approximately (packed fused multiply-adds) and held in FP16,
-                                   summed in FP32; the GBIVF_MIXED_SCAN_ALPHA * k best (at most 4096) are re-scored
-                                   in the reference's FP32 arithmetic, so every returned distance is the
-                                   plain form's and the ids match it unless a true neighbour fell outside
-                                   the approximate selection */
+                                   summed in FP32; of the GBIVF_MIXED_SCAN_ALPHA * k best (at most 4096),
+                                   those within the tables' error bound of the k-th exact distance are
+                                   re-scored in the reference's FP32 arithmetic, so every returned distance
+                                   is the plain form's and the ids match it unless a true neighbour fell
+                                   outside the approximate selection (gbivf_last_unproven counts the
+                                   queries where that could not be excluded) */
 #define GBIVF_MIXED_SCAN_ALPHA 4
 #define GBIVF_RERANK_REFINE 0x20u /* re-rank the kl ADC candidates by the distance to their refined
                                      reconstruction y + c1(codes) + c2(refinement codes) instead of the
@@ -221,6 +223,17 @@ int gbivf_last_stages_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms, floa
  * ran list by list. Either array may be NULL. Waits for the search. No
  * counterpart in the reference. */
 int gbivf_last_scan_parts(gbivf_index *ix, float *parts_ms, int64_t *counters);
+
+/* The number of queries of the last search with GBIVF_MIXED_SCAN whose result
+ * the precision form could not prove identical to the exact form's (0 after a
+ * search without it). The precision form re-scores, in the reference's FP32
+ * arithmetic, every approximate candidate whose approximate distance lies
+ * within the FP16 tables' error bound of the k-th (kl-th) exact distance; a
+ * query is proven when all such candidates were among the GBIVF_MIXED_SCAN_ALPHA
+ * * k approximate best it kept. Read once the search has completed (after the
+ * host call returns, or after the caller synchronised a device search's
+ * stream). No counterpart in the reference. */
+int gbivf_last_unproven(gbivf_index *ix, int64_t *queries);
 
 /* The coarse stage alone: knn_full(2, nq, C, d, w, coa, queries, ...)
  * (sequential/ivf_pq/ivf_search.cpp:37-38): the w nearest lists per query,

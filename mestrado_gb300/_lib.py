@@ -34,7 +34,7 @@ EXPORTS = [
     "gbivf_graph_destroy", "gbivf_graph_kernel_count", "gbivf_index_autotune", "gbivf_generate_mixture", "gbivf_kmeans", "gbivf_assign",
     "gbivf_pq_train", "gbivf_pq_encode", "gbivf_last_coarse_stats", "gbivf_coarse_assign_device",
     "gbivf_index_set_refine", "gbivf_index_set_refine_device", "gbivf_pq_error", "gbivf_index_create_device",
-    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_last_scan_parts", "gbivf_selftest_wait_timeout", "gbivf_index_scan_form",
+    "gbivf_assign_flags", "gbivf_last_stages_ms", "gbivf_last_scan_parts", "gbivf_last_unproven", "gbivf_selftest_wait_timeout", "gbivf_index_scan_form",
 ]
 
 
@@ -72,6 +72,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.gbivf_last_stage_ms.argtypes = [vp, vp, vp]
     lib.gbivf_last_stages_ms.argtypes = [vp, vp, vp, vp]
     lib.gbivf_last_scan_parts.argtypes = [vp, vp, vp]
+    lib.gbivf_last_unproven.argtypes = [vp, vp]
     lib.gbivf_index_scan_form.argtypes = [vp, vp, vp]
     lib.gbivf_selftest_wait_timeout.argtypes = [C.c_int, vp, vp, vp]
     lib.gbivf_coarse_assign_noalloc.argtypes = [vp, vp, i32, i32, vp, vp, vp]

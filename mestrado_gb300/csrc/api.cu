@@ -131,8 +131,10 @@ struct gbivf_index {
     DBuf coa_tiles, coa_len, coa_colG, coa_colK, w_qtiles, w_flags;
     // filtered coarse stage (large C): per-query bounds, counters, candidate slots, GEMM survivors
     DBuf w_thr, w_fcnt, w_cand, w_surv, w_scnt;
-    // hand-off lists of the precision form and the refinement re-rank
-    DBuf w_clist;
+    // hand-off lists of the precision form and the refinement re-rank; the precision form's count of
+    // queries whose result its finalize could not prove equal to the exact form's
+    DBuf w_clist, w_unproven;
+    bool last_mixed = false;          // the last search used the precision form of the scan
     // list-centric scan (scan_lists.cu): one workspace block, its layout, stage events
     DBuf lc_ws;
     ListScanWork lcw;
@@ -171,7 +173,7 @@ void free_index(gbivf_index* ix) {
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
                     &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->w_clist,
-                    &ix->pq2, &ix->codes2, &ix->lc_ws})
+                    &ix->w_unproven, &ix->pq2, &ix->codes2, &ix->lc_ws})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -265,6 +267,13 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
         pn[e] = norm_d_host(pq + (int64_t)e * ds, ds);
         split_norm(pn[e], &phi[e], &plo[e]);
     }
+    // the precision form's error bound uses sum_s max_c ||c_s||^2 (rounded up)
+    double cmax = 0.0;
+    for (int sq = 0; sq < nsq; sq++) {
+        double mx = 0.0;
+        for (int c = 0; c < ks; c++) mx = std::max(mx, pn[(size_t)sq * ks + c]);
+        cmax += mx;
+    }
     if (cudaDeviceGetAttribute(&ix->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) ix->num_sms = 1;
     if (const char* v = getenv("GBIVF_SCAN_THREADS")) ix->scan_threads = atoi(v) == 1024 ? 1024 : 512;
     // a smaller emission buffer than the default sends more queries through the overflow pass
@@ -333,6 +342,7 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     dx.pq_norm = p_pn;
     dx.pq_hi = p_phi;
     dx.pq_lo = p_plo;
+    dx.pq_cmax = (float)(cmax * (1.0 + 0x1p-20));
     dx.list_beg = p_beg;
     dx.list_len = p_len;
     dx.codes = p_codes;
@@ -415,6 +425,7 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
     CK(ix->w_queue.ensure(sizeof(int)));
     a.queue = ix->w_queue.as<int>();
     const bool mixed = a.flags & SCAN_MIXED;
+    ix->last_mixed = mixed;
     if (mixed) {
         a.sel_mult = GBIVF_MIXED_SCAN_ALPHA;
         a.sel_cap = 4096;
@@ -442,6 +453,11 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
         if (mixed || refine) {
             CK(ix->w_clist.ensure(sizeof(int32_t) * (size_t)a.nq * stride));
             a.cand_list = ix->w_clist.as<int32_t>();
+        }
+        if (mixed) {
+            CK(ix->w_unproven.ensure(sizeof(int)));
+            CK(cudaMemsetAsync(ix->w_unproven.p, 0, sizeof(int), st));
+            a.unproven = ix->w_unproven.as<int>();
         }
         if (lists) {
             if (!(a.flags & (SCAN_MIXED | SCAN_REFINE))) {  // the select kernel writes lists only for those
@@ -1015,6 +1031,18 @@ int gbivf_last_scan_parts(gbivf_index* ix, float* parts_ms, int64_t* counters) {
             counters[3] = 1;
         }
     }
+    return GBIVF_OK;
+}
+
+int gbivf_last_unproven(gbivf_index* ix, int64_t* queries) {
+    if (!ix || !queries) return fail(GBIVF_ERR_INVALID, "index or output is NULL");
+    DeviceGuard g(ix->device);
+    *queries = 0;
+    if (!ix->last_mixed || !ix->w_unproven.p) return GBIVF_OK;
+    int h = 0;
+    CK(cudaStreamSynchronize(ix->stream));
+    CK(cudaMemcpy(&h, ix->w_unproven.p, sizeof(int), cudaMemcpyDeviceToHost));
+    *queries = h;
     return GBIVF_OK;
 }
 

@@ -241,6 +241,187 @@ __device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B,
     }
 }
 
+// The K-th smallest (1-based, 1 <= K <= their count) of the unique keys A[i], i < n, whose bit i is
+// set in flags (every key when flags is NULL), by the same radix select as block_kth: 8-bit digits
+// from the highest bit in which those keys differ, until one key is left in the digit's bucket.
+// All threads of the block call it; it ends with a barrier.
+__device__ inline u64 block_kth_flagged(const u64* A, int n, const unsigned* flags, int K) {
+    __shared__ int hist[2][256];
+    __shared__ int info[2][4];
+    __shared__ u64 red[3];  // the smallest key, the OR of the differences to it, the last survivor
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+    auto in = [&](int i) { return !flags || ((flags[i >> 5] >> (i & 31)) & 1u); };
+    if (tid == 0) {
+        red[0] = KEY_MAX;
+        red[1] = 0;
+    }
+    for (int i = tid; i < 256; i += nt) hist[0][i] = 0;
+    __syncthreads();
+    u64 lo = KEY_MAX;
+    for (int i = tid; i < n; i += nt)
+        if (in(i)) lo = A[i] < lo ? A[i] : lo;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const u64 x = __shfl_xor_sync(0xffffffffu, lo, o);
+        lo = x < lo ? x : lo;
+    }
+    if (lane == 0) atomicMin(&red[0], lo);
+    __syncthreads();
+    const u64 ref = red[0];
+    u64 acc = 0;
+    for (int i = tid; i < n; i += nt)
+        if (in(i)) acc |= A[i] ^ ref;
+    const unsigned alo = __reduce_or_sync(0xffffffffu, (unsigned)acc);
+    const unsigned ahi = __reduce_or_sync(0xffffffffu, (unsigned)(acc >> 32));
+    if (lane == 0 && (alo | ahi)) atomicOr(&red[1], ((u64)ahi << 32) | alo);
+    __syncthreads();
+    const u64 diff = red[1];
+    if (diff == 0) return ref;  // a single key
+    int hib = 63 - __clzll((long long)diff);
+    u64 kmask = hib == 63 ? 0ull : (~0ull << (hib + 1));
+    u64 kval = ref & kmask;
+    int want = K;
+    for (int p = 0;; p++) {
+        int* h = hist[p & 1];
+        int* inf = info[p & 1];
+        const int lob = max(hib - 7, 0);
+        const int width = hib - lob + 1;
+        const u64 dmask = (1ull << width) - 1ull;
+        for (int i = tid; i < n; i += nt)
+            if (in(i) && (A[i] & kmask) == kval) atomicAdd(&h[(A[i] >> lob) & dmask], 1);
+        // the next pass's histogram: its last reader, the previous pass's scan, finished before the
+        // previous pass's second barrier
+        for (int i = tid; i < 256; i += nt) hist[(p + 1) & 1][i] = 0;
+        __syncthreads();
+        if (tid < 32) {
+            int c[8], sum = 0;  // lane owns bins 8 lane .. 8 lane + 7
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                c[j] = h[8 * lane + j];
+                sum += c[j];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            int before = incl - sum;
+            if (before < want && want <= incl) {
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (before < want && want <= before + c[j]) {
+                        inf[0] = 8 * lane + j;
+                        inf[1] = want - before;
+                        inf[2] = c[j];
+                    }
+                    before += c[j];
+                }
+            }
+        }
+        __syncthreads();
+        const int dig = inf[0], cnt = inf[2];
+        want = inf[1];
+        kmask |= dmask << lob;
+        kval |= (u64)dig << lob;
+        if (lob == 0) return kval;  // all 64 bits known
+        if (cnt == 1) {
+            for (int i = tid; i < n; i += nt)
+                if (in(i) && (A[i] & kmask) == kval) red[2] = A[i];
+            __syncthreads();
+            const u64 r = red[2];
+            __syncthreads();
+            return r;
+        }
+        hib = lob - 1;
+    }
+}
+
+// Ascending order of q <= NT * PER unique keys sk[0..q) with their payloads ss[0..q), by a bitonic
+// network over NT * PER elements (KEY_MAX padding) held in registers, PER consecutive elements per
+// thread: partners within a thread are exchanged in registers, within a warp by shuffles, and only
+// the stages across warps go through shared memory (sk, ss). blockDim.x == NT. Ends with a barrier.
+template <int NT, int PER>
+__device__ inline void block_sort_regs(u64* sk, int32_t* ss, int q) {
+    constexpr int CAP = NT * PER;
+    constexpr int LOG = __builtin_ctz(CAP);
+    static_assert((CAP & (CAP - 1)) == 0 && (PER & (PER - 1)) == 0 && NT % 32 == 0, "powers of two");
+    const int tid = threadIdx.x;
+    u64 k[PER];
+    int32_t v[PER];
+#pragma unroll
+    for (int e = 0; e < PER; e++) {
+        const int i = tid * PER + e;
+        k[e] = i < q ? sk[i] : KEY_MAX;
+        v[e] = i < q ? ss[i] : 0;
+    }
+#pragma unroll
+    for (int ls = 1; ls <= LOG; ls++) {
+        const int size = 1 << ls;
+#pragma unroll
+        for (int lj = ls - 1; lj >= 0; lj--) {
+            const int j = 1 << lj;
+            if (j < PER) {
+#pragma unroll
+                for (int e = 0; e < PER; e++) {
+                    if ((e & j) == 0) {
+                        const int e2 = e | j;
+                        const bool asc = ((tid * PER + e) & size) == 0;
+                        if ((k[e] > k[e2]) == asc) {
+                            const u64 tk = k[e];
+                            k[e] = k[e2];
+                            k[e2] = tk;
+                            const int32_t tv = v[e];
+                            v[e] = v[e2];
+                            v[e2] = tv;
+                        }
+                    }
+                }
+            } else {
+                const bool cross = j >= 32 * PER;
+                if (cross) {
+                    __syncthreads();  // the previous cross stage's readers are done
+#pragma unroll
+                    for (int e = 0; e < PER; e++) {
+                        sk[tid * PER + e] = k[e];
+                        ss[tid * PER + e] = v[e];
+                    }
+                    __syncthreads();
+                }
+                const bool lower = ((tid * PER) & j) == 0;
+#pragma unroll
+                for (int e = 0; e < PER; e++) {
+                    const bool asc = ((tid * PER + e) & size) == 0;
+                    u64 ok;
+                    int32_t ov;
+                    if (cross) {
+                        ok = sk[(tid * PER + e) ^ j];
+                        ov = ss[(tid * PER + e) ^ j];
+                    } else {
+                        ok = __shfl_xor_sync(0xffffffffu, k[e], j / PER);
+                        ov = __shfl_xor_sync(0xffffffffu, v[e], j / PER);
+                    }
+                    const bool take = (lower == asc) ? ok < k[e] : ok > k[e];
+                    if (take) {
+                        k[e] = ok;
+                        v[e] = ov;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();  // the last cross stage's readers are done
+#pragma unroll
+    for (int e = 0; e < PER; e++) {
+        const int i = tid * PER + e;
+        if (i < q) {
+            sk[i] = k[e];
+            ss[i] = v[e];
+        }
+    }
+    __syncthreads();
+}
+
 // Merge the nb buffered keys into the best set. nb is block-uniform.
 __device__ inline void topk_flush(TopKSmem& s, int nb) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;

@@ -26,6 +26,7 @@ struct DevIndex {
     const double* pq_norm = nullptr;   // m x ks double norms (b-operand of the table product)
     const float* pq_hi = nullptr;      // m x ks  RN32(pq_norm)
     const float* pq_lo = nullptr;      // m x ks  RN32(pq_norm - pq_hi)
+    float pq_cmax = 0.0f;              // sum over sub-quantizers of the largest centroid norm (rounded up)
     const int64_t* list_beg = nullptr; // C   first row of each list
     const int32_t* list_len = nullptr; // C
     const uint8_t* codes = nullptr;    // rows x m
@@ -74,6 +75,9 @@ struct ScanArgs {
     const int* nqlist = nullptr;
     // SCAN_KEYS_ONLY: per query the k-th best key when k were found, else KEY_MAX
     unsigned long long* tau_out = nullptr;
+    // precision form: incremented by finalize for each query whose result it could not prove equal
+    // to the exact form's (NULL: not counted)
+    int* unproven = nullptr;
 };
 
 // per-query shape of a (possibly uneven) batch

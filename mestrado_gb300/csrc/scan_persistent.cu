@@ -577,6 +577,13 @@ constexpr int FIN_NT = 128;
 // element, two barriers), larger ones by a bitonic network (log^2 barriers, fewer operations)
 constexpr int RANK_SORT_MAX = 256;
 constexpr int FIN_NT_BIG = 512;
+// the precision form's error bound (finalize_kernel): relative, then absolute per unit of
+// ||r||^2 + sum_s max_c ||c_s||^2, then absolute (FP16 subnormals)
+constexpr double MIX_DELTA = 0x1p-9;
+constexpr double MIX_EPS_REL = 0x1p-12;
+constexpr double MIX_EPS_ABS = 0x1p-12;
+// the precision form's final sort: keys per thread of the register bitonic network
+constexpr int FIN_SORT_PER = 8;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -709,7 +716,7 @@ __device__ __forceinline__ void refine_rerank(const DevIndex& ix, const ScanArgs
 // The sort carries the keys and, with them, either base ids (the exact form) or hand-off slots
 // (precision form, refinement re-rank: the slot leads to the candidate's code row and list).
 template <bool MIXED, int M, int NT>
-__global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
+__global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 3) : 0) finalize_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     constexpr int FIN_NT = NT;
     const int n2 = a.cand_stride;  // power of two
@@ -726,28 +733,136 @@ __global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
     int p2 = 2;
     while (p2 < n) p2 <<= 1;
     for (int c = tid; c < p2; c += FIN_NT) {
-        keys[c] = a.cand_key[hb + c];
+        keys[c] = c < n ? a.cand_key[hb + c] : KEY_MAX;
         ids[c] = slots ? c : a.cand_id[hb + c];
     }
     if (rerank || slots)
         for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
     __syncthreads();
     if constexpr (MIXED) {
-        // exact re-score of the alpha*k approximate candidates, keyed (distance, position) as
-        // the plain form keys them; the exact top-k (or top-kl) is then the plain form's
-        // whenever it lies among the candidates
-        for (int c = tid; c < p2; c += FIN_NT) {
-            u64 key = KEY_MAX;
-            if (c < n) {
-                const float dist = exact_adc<M>(ix, xq, a.cand_list[hb + c], a.cand_id[hb + c]);
-                key = make_key(dist, key_payload(keys[c]));
+        // Exact re-score of the approximate candidates that can still belong to the exact top-kk,
+        // keyed (distance, position) as the plain form keys them. Every approximate distance A
+        // bounds the exact one E from below: E >= A (1 - MIX_DELTA) - eps_q, where MIX_DELTA covers
+        // the FP16 rounding of the table entries (2^-11 relative, summed in FP32) and eps_q the FP32
+        // rounding of both forms' expansions (at most ~2^-16 (||r||^2 + sum_s max ||c_s||^2)), with
+        // a margin of 4 and 16. So, with T0 the largest exact distance of the kk best approximate
+        // candidates, no candidate with A >= tau = (T0 + eps_q) / (1 - MIX_DELTA) can enter the
+        // exact top-kk: those below tau are re-scored, the rest are not.
+        // Neither set is sorted: the kk-th approximate key is found by a radix select, the
+        // candidates to re-score are gathered into a list (ids[], whose identity contents this form
+        // does not need), and only the final kk exact keys are sorted, in registers.
+        static_assert(NT == FIN_NT && NT * FIN_SORT_PER >= 1024, "the final sort holds kl <= 1024 keys");
+        u64* sk = reinterpret_cast<u64*>(xq + 128);              // the final sort's staging (d = 128)
+        int32_t* ss = reinterpret_cast<int32_t*>(sk + NT * FIN_SORT_PER);
+        int32_t* list = ids;
+        const int kk0 = (rerank || refine) ? a.kl : query_k(a, q);
+        const int ksel = min(kk0 * a.sel_mult, a.sel_cap);
+        const int kk = min(n, kk0);
+        const int lane = tid & 31;
+        __shared__ unsigned s_flag[4096 / 32];  // bit c: candidate c re-scored (n <= sel_cap <= 4096)
+        __shared__ u64 s_t0, s_amax;
+        __shared__ unsigned s_r2;
+        __shared__ int s_cnt, s_cnt2;
+        for (int i = tid; i < 4096 / 32; i += NT) s_flag[i] = 0u;
+        if (tid == 0) {
+            s_t0 = 0;
+            s_amax = 0;
+            s_r2 = 0u;
+            s_cnt = 0;
+            s_cnt2 = 0;
+        }
+        u64 amax = 0;
+        for (int c = tid; c < n; c += NT) amax = keys[c] > amax ? keys[c] : amax;
+        __syncthreads();
+        atomicMax(&s_amax, amax);
+        const u64 th = n > kk ? block_kth_flagged(keys, n, nullptr, kk) : KEY_MAX;
+        // gather the candidates passing `pred` into list[s_cnt ..) and mark them (warp-uniform
+        // loop: each 32-candidate word of the marks belongs to one warp)
+        auto gather = [&](auto pred) {
+            for (int c0 = tid & ~31; c0 < n; c0 += NT) {
+                const int c = c0 + lane;
+                const bool in = c < n && pred(c);
+                const unsigned m = __ballot_sync(0xffffffffu, in);
+                if (m == 0u) continue;
+                int base = 0;
+                if (lane == 0) {
+                    base = atomicAdd(&s_cnt, __popc(m));
+                    s_flag[c0 >> 5] |= m;
+                }
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (in) list[base + __popc(m & ((1u << lane) - 1u))] = c;
             }
-            keys[c] = key;
+        };
+        auto rescore = [&](int c) {
+            keys[c] = make_key(exact_adc<M>(ix, xq, a.cand_list[hb + c], a.cand_id[hb + c]), key_payload(keys[c]));
+            return keys[c];
+        };
+        gather([&](int c) { return keys[c] <= th; });
+        __syncthreads();
+        const int m0 = s_cnt;
+        u64 t0 = 0;
+        for (int i = tid; i < m0; i += NT) {
+            const u64 key = rescore(list[i]);
+            t0 = key > t0 ? key : t0;
+        }
+        // the largest squared residual norm over the query's probes (a bound on ||r||^2 for every
+        // candidate, handed off or not)
+        float r2 = 0.0f;
+        for (int j = tid; j < query_w(a, q); j += NT) {
+            const int l = a.probes[(int64_t)q * a.w + j];
+            if (l < 0 || l >= ix.C) continue;
+            const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128);
+            float sq = 0.0f;
+#pragma unroll 8
+            for (int v = 0; v < 32; v++) {
+                const float4 y = __ldg(y4 + v);
+                const float d0 = xq[4 * v] - y.x, d1 = xq[4 * v + 1] - y.y, d2 = xq[4 * v + 2] - y.z,
+                            d3 = xq[4 * v + 3] - y.w;
+                sq = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, sq))));
+            }
+            r2 = fmaxf(r2, sq);
+        }
+        atomicMax(&s_t0, t0);
+        atomicMax(&s_r2, __float_as_uint(r2));  // (non-negative floats order as their bits)
+        __syncthreads();
+        const double T0 = fmax(0.0, (double)key_dist(s_t0));
+        const double eps = MIX_EPS_REL * ((double)__uint_as_float(s_r2) * (1.0 + 0x1p-10) + (double)ix.pq_cmax) +
+                           MIX_EPS_ABS;
+        const double tau = (T0 + eps) / (1.0 - MIX_DELTA) * (1.0 + 0x1p-20);
+        // the rest of the candidates below tau (their keys are still approximate)
+        gather([&](int c) { return !((s_flag[c >> 5] >> (c & 31)) & 1u) && (double)key_dist(keys[c]) < tau; });
+        __syncthreads();
+        const int m = s_cnt;
+        for (int i = m0 + tid; i < m; i += NT) rescore(list[i]);
+        // not proven: the hand-off is full (candidates may lie beyond it) and all of it is below tau
+        if (tid == 0 && a.unproven && n >= ksel && (double)key_dist(s_amax) < tau) atomicAdd(a.unproven, 1);
+        __syncthreads();
+        // the kk best exact keys of the re-scored set, in order
+        const u64 th2 = m > kk ? block_kth_flagged(keys, n, s_flag, kk) : KEY_MAX;
+        for (int c0 = tid & ~31; c0 < n; c0 += NT) {
+            const int c = c0 + lane;
+            const bool in = c < n && ((s_flag[c >> 5] >> (c & 31)) & 1u) && keys[c] <= th2;
+            const unsigned mk = __ballot_sync(0xffffffffu, in);
+            if (mk == 0u) continue;
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&s_cnt2, __popc(mk));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (in) {
+                const int o = base + __popc(mk & ((1u << lane) - 1u));
+                sk[o] = keys[c];
+                ss[o] = c;
+            }
         }
         __syncthreads();
-        if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);  // (the KEY_MAX padding stays past n)
-        else bitonic_sort_pairs(keys, ids, p2);
-        n = min(n, (rerank || refine) ? a.kl : query_k(a, q));
+        const int nout = s_cnt2;  // min(m, kk): the keys are unique
+        if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
+        else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, nout);
+        for (int c = tid; c < nout; c += NT) {
+            keys[c] = sk[c];
+            ids[c] = ss[c];
+        }
+        __syncthreads();
+        n = nout;
     } else {
         if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);
         else bitonic_sort_pairs(keys, ids, p2);
@@ -835,7 +950,8 @@ int scan_persistent_stride(const ScanArgs& a) {
 
 template <int M, bool MIXED>
 static cudaError_t launch_fin(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
-    const size_t fsm = (size_t)a.cand_stride * 12 + 512;  // keys, ids, the query
+    // keys, ids, the query; the precision form's final sort staging
+    const size_t fsm = (size_t)a.cand_stride * 12 + 512 + (MIXED ? (size_t)FIN_NT * FIN_SORT_PER * 12 : 0);
     const bool big = !MIXED && (a.flags & SCAN_REFINE);
     void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
     if constexpr (!MIXED)

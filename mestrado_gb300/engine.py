@@ -244,6 +244,13 @@ class GpuIndex:
         names = ["plan", "first_pass", "grouping", "list_scan", "select", "overflow_pass", "finalize"]
         return dict(zip(names, list(p))), dict(zip(["pairs", "items", "overflowed", "list_scan"], list(c)))
 
+    def last_unproven(self):
+        """Queries of the last precision-form search whose result was not proven identical to the
+        exact form's (gbivf_last_unproven); 0 after a search in the exact form."""
+        n = C.c_int64()
+        check(self.lib.gbivf_last_unproven(self.h, C.byref(n)))
+        return n.value
+
     def coarse_assign(self, queries, w, mixed=False, stats=False, full=False):
         """knn_full over the coarse centroids: (coaidx, coadis) nq x w. With
         mixed=True the tensor-core form runs, with full=True the full-block

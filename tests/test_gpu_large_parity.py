@@ -10,7 +10,8 @@ The plain form must return the oracle's ids and distance bits on every
 sampled query (both keyed by (distance, position in the probe order)); the
 sample holds the queries with the largest k and nprobe. The precision form
 returns exact distances for every id it returns (bit-identical to the plain
-form's), and its ids are the plain form's on (at least) 99% of the queries."""
+form's), and its ids are the plain form's on (at least) 99% of the queries and on every query
+it reports as proven."""
 import numpy as np
 import pytest
 
@@ -48,6 +49,7 @@ def _check(ix, q, wq, kq, nsample):
     gi = GpuIndex(ix)
     p_ids, p_dis, off = gi.search_batched(q, wq, kq)
     m_ids, m_dis, _ = gi.search_batched(q, wq, kq, mixed_coarse=True, mixed_scan=True)
+    unproven = gi.last_unproven()
     gi.close()
     sel = _sample(wq, kq, nsample)
     o_ids, o_dis, o_off = oracle.search_batched(ix, q[sel], wq[sel], kq[sel], nthreads=16)
@@ -62,7 +64,9 @@ def _check(ix, q, wq, kq, nsample):
         pd = dict(zip(a.tolist(), p_dis[off[i]:off[i + 1]].view(np.uint32).tolist()))
         for x, y in zip(b.tolist(), m_dis[off[i]:off[i + 1]].view(np.uint32).tolist()):
             assert x < 0 or x not in pd or pd[x] == y, f"query {i}: id {x} distance differs between the forms"
+    print(f"precision form: {same} of {len(q)} rows identical, {unproven} queries not proven")
     assert same >= 0.99 * len(q), (same, len(q))
+    assert len(q) - same <= unproven, (same, unproven, len(q))
     return sel
 
 

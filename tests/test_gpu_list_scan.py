@@ -8,8 +8,9 @@ distances) and the oracle's (keyed tie rule). Precision form: its approximate
 sums run in a row-rotated order (rot_codes.cuh), so its candidate sets may
 differ from the per-query kernel's in the last bits; what must hold is what
 the form promises -- every returned distance is the exact one (bit-identical
-to the exact form's for the same id) and the ids are the exact form's on at
-least 99% of the queries. Covered on the golden cases, on uneven batches with
+to the exact form's for the same id), the ids are the exact form's on every
+query that the form reports as proven (all but gbivf_last_unproven of them)
+and on at least 99% of the queries. Covered on the golden cases, on uneven batches with
 k up to 1000, on a GPU-built index with a few thousand queries, through the
 overflow pass (a tiny emission buffer) and inside a CUDA graph (a replay
 returns exactly what the direct call returns)."""
@@ -34,9 +35,9 @@ def _rows(x, off):
     return [x[off[i]:off[i + 1]] for i in range(len(off) - 1)]
 
 
-def _precision(m, e, what, off=None):
+def _precision(m, e, what, off=None, unproven=0):
     """The precision form's result m against the exact form's e: the same distance bits for every id both
-    return, the same ids on at least 99% of the queries."""
+    return, the same ids on every query but (at most) the `unproven` ones and on at least 99% of them."""
     mi, md, ei, ed = _rows(m[0], off), _rows(m[1], off), _rows(e[0], off), _rows(e[1], off)
     same = 0
     for q in range(len(mi)):
@@ -45,6 +46,7 @@ def _precision(m, e, what, off=None):
         for i, d in zip(mi[q].tolist(), md[q].view(np.uint32).tolist()):
             assert i < 0 or i not in ex or ex[i] == d, f"{what}: query {q} id {i} distance differs"
     assert same >= 0.99 * len(mi), f"{what}: identical rows {same} of {len(mi)}"
+    assert len(mi) - same <= unproven, f"{what}: {len(mi) - same} rows differ, {unproven} not proven"
 
 
 @pytest.mark.parametrize("name", ["cfg1", "m16"])
@@ -61,8 +63,8 @@ def test_golden_cases_list_equals_query_and_oracle(name):
         o = oracle.ivfpq_search(g.ix, g.queries, k=k, kl=kl, w=w, base=g.base if rerank else None, rerank=rerank,
                                 ties=oracle.TIES_KEYED)
         _same(lst, o, f"{what} vs oracle")
-        _precision(gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=True, scan_order="lists"), lst,
-                   f"{what} precision form")
+        mix = gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=True, scan_order="lists")
+        _precision(mix, lst, f"{what} precision form", unproven=gi.last_unproven())
     gi.close()
 
 
@@ -92,7 +94,7 @@ def test_uneven_batches(name):
     o_ids, o_dis, _ = oracle.search_batched(g.ix, g.queries, wq, kq)
     _same(lst[:2], (o_ids, o_dis), f"{name} vs oracle")
     mix = gi.search_batched(g.queries, wq, kq, mixed_coarse=True, mixed_scan=True, scan_order="lists")
-    _precision(mix[:2], lst[:2], f"{name} precision form", off=lst[2])
+    _precision(mix[:2], lst[:2], f"{name} precision form", off=lst[2], unproven=gi.last_unproven())
     gi.close()
 
 
@@ -128,7 +130,9 @@ def test_gpu_built_index_list_equals_query(built):
     lst = gi.search_batched(q, wq, kq, scan_order="lists")
     _same(lst[:2], gi.search_batched(q, wq, kq, scan_order="queries")[:2], "exact form")
     mix = gi.search_batched(q, wq, kq, mixed_coarse=True, mixed_scan=True, scan_order="lists")
-    _precision(mix[:2], lst[:2], "precision form", off=lst[2])
+    u = gi.last_unproven()
+    print(f"precision form: {u} of {len(q)} queries not proven")
+    _precision(mix[:2], lst[:2], "precision form", off=lst[2], unproven=u)
     # and a uniform batch with re-rank-free k = 100, w = 32
     lst = gi.search(q, 100, 32, scan_order="lists")
     qry = gi.search(q, 100, 32, scan_order="queries")
@@ -168,7 +172,7 @@ def test_overflow_pass(built, monkeypatch):
         assert counters["list_scan"] == 1 and counters["overflowed"] > len(q) // 4, counters
         got = (d_ids.cpu().numpy(), d_dis.cpu().numpy())
         if mixed:
-            _precision(got, expect[:2], "overflow, precision form", off=off)
+            _precision(got, expect[:2], "overflow, precision form", off=off, unproven=gi.last_unproven())
         else:
             _same(got, expect[:2], "overflow, exact form")
     gi.close()

@@ -1,7 +1,9 @@
 """Precision form of the scan (GB300): FP16 approximate tables summed in FP32,
-then the alpha*k best re-scored in the reference's FP32 arithmetic. Every
-returned distance must be the plain form's for that id; ids match the plain
-form's except where a true neighbour fell outside the approximate selection."""
+then, of the alpha*k best, those within the tables' error bound of the k-th
+exact distance re-scored in the reference's FP32 arithmetic. Every returned
+distance must be the plain form's for that id; ids match the plain form's on
+every query the form reports as proven, and may differ elsewhere only where a
+true neighbour fell outside the approximate selection."""
 import numpy as np
 import pytest
 
@@ -36,9 +38,11 @@ def test_mixed_scan_golden(name, rerank):
         a = gi.search(g.queries, k, w, kl=kl, rerank=rerank)
         b = gi.search(g.queries, k, w, kl=kl, rerank=rerank, mixed_scan=True)
         same, ok = compare(a[0], a[1], b[0], b[1])
-        print(f"[{name} rerank={rerank} k={k}] identical rows {same:.4f}")
+        u = gi.last_unproven()
+        print(f"[{name} rerank={rerank} k={k}] identical rows {same:.4f}, {u} not proven")
         assert ok, "a returned distance differs from the plain form's"
         assert same >= 0.99
+        assert round((1.0 - same) * len(g.queries)) <= u
     gi.close()
 
 
@@ -53,12 +57,14 @@ def test_mixed_scan_uneven_batch_and_both_mixed_forms():
     gi = GpuIndex(g.ix)
     a_ids, a_dis, off = gi.search_batched(g.queries, wq, kq)
     b_ids, b_dis, _ = gi.search_batched(g.queries, wq, kq, mixed_coarse=True, mixed_scan=True)
+    u = gi.last_unproven()
     rows = [(a_ids[off[i]:off[i + 1]], a_dis[off[i]:off[i + 1]], b_ids[off[i]:off[i + 1]], b_dis[off[i]:off[i + 1]])
             for i in range(nq)]
     same = np.mean([np.array_equal(r[0], r[2]) for r in rows])
     ok = all(compare(r[0], r[1], r[2], r[3])[1] for r in rows)
-    print(f"uneven: identical rows {same:.4f}")
+    print(f"uneven: identical rows {same:.4f}, {u} not proven")
     assert ok and same >= 0.99
+    assert round((1.0 - same) * nq) <= u
     gi.close()
 
 
@@ -76,11 +82,29 @@ def test_mixed_scan_on_gpu_built_zipf_index():
     for k, w in ((100, 32), (1000, 64)):
         a = gi.search(q, k, w)
         b = gi.search(q, k, w, mixed_scan=True, mixed_coarse=True)
+        u = gi.last_unproven()
         same, ok = compare(a[0], a[1], b[0], b[1])
+        assert round((1.0 - same) * len(q)) <= u
         recall = np.mean([len(set(x) & set(y)) / k for x, y in zip(a[0], b[0])])
         print(f"k={k} w={w}: identical rows {same:.4f}, overlap with plain {recall:.5f}")
         assert ok
         assert recall >= 0.998
+    gi.close()
+
+
+def test_unproven_count_follows_the_last_search():
+    """gbivf_last_unproven: 0 after an exact-form search; after a precision-form search with an
+    approximate selection of alpha * k, a count between 0 and the number of queries."""
+    from mestrado_gb300.engine import GpuIndex
+
+    g = golden_cases.load("m16")
+    gi = GpuIndex(g.ix)
+    w = g.meta["w"]
+    gi.search(g.queries, 10, w, mixed_scan=True)
+    u = gi.last_unproven()
+    assert 0 <= u <= len(g.queries)
+    gi.search(g.queries, 10, w)
+    assert gi.last_unproven() == 0
     gi.close()
 
 
@@ -124,8 +148,10 @@ def test_mixed_scan_long_lists_every_shape(long_list_indexes, m, threads, monkey
     for k, w in ((10, 3), (100, 8)):
         a = gi.search(q, k, w)
         b = gi.search(q, k, w, mixed_scan=True)
+        u = gi.last_unproven()
         same, ok = compare(a[0], a[1], b[0], b[1])
-        print(f"m={m} threads={threads} k={k} w={w}: identical rows {same:.4f}")
+        print(f"m={m} threads={threads} k={k} w={w}: identical rows {same:.4f}, {u} not proven")
+        assert round((1.0 - same) * len(q)) <= u
         assert ok, "a returned distance differs from the plain form's"
         assert same >= 0.99
     gi.close()
