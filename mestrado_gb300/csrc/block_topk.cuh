@@ -245,7 +245,7 @@ __device__ inline u64 block_kth(TopKSmem& s, const u64* A, int na, const u64* B,
 // set in flags (every key when flags is NULL), by the same radix select as block_kth: 8-bit digits
 // from the highest bit in which those keys differ, until one key is left in the digit's bucket.
 // All threads of the block call it; it ends with a barrier.
-__device__ inline u64 block_kth_flagged(const u64* A, int n, const unsigned* flags, int K) {
+static __device__ __noinline__ u64 block_kth_flagged(const u64* A, int n, const unsigned* flags, int K) {
     __shared__ int hist[2][256];
     __shared__ int info[2][4];
     __shared__ u64 red[3];  // the smallest key, the OR of the differences to it, the last survivor
@@ -342,10 +342,9 @@ __device__ inline u64 block_kth_flagged(const u64* A, int n, const unsigned* fla
 // thread: partners within a thread are exchanged in registers, within a warp by shuffles, and only
 // the stages across warps go through shared memory (sk, ss). blockDim.x == NT. Ends with a barrier.
 template <int NT, int PER>
-__device__ inline void block_sort_regs(u64* sk, int32_t* ss, int q) {
+__device__ __noinline__ void block_sort_regs(u64* sk, int32_t* ss, int q) {
     constexpr int CAP = NT * PER;
-    constexpr int LOG = __builtin_ctz(CAP);
-    static_assert((CAP & (CAP - 1)) == 0 && (PER & (PER - 1)) == 0 && NT % 32 == 0, "powers of two");
+    static_assert((CAP & (CAP - 1)) == 0 && (PER & (PER - 1)) == 0 && PER >= 2 && NT % 32 == 0, "powers of two");
     const int tid = threadIdx.x;
     u64 k[PER];
     int32_t v[PER];
@@ -355,60 +354,62 @@ __device__ inline void block_sort_regs(u64* sk, int32_t* ss, int q) {
         k[e] = i < q ? sk[i] : KEY_MAX;
         v[e] = i < q ? ss[i] : 0;
     }
+    // one compare-exchange of registers e < e2 in the direction of merge size `size`
+    auto cx = [&](int e, int e2, int size) {
+        const bool asc = ((tid * PER + e) & size) == 0;
+        if ((k[e] > k[e2]) == asc) {
+            const u64 tk = k[e];
+            k[e] = k[e2];
+            k[e2] = tk;
+            const int32_t tv = v[e];
+            v[e] = v[e2];
+            v[e2] = tv;
+        }
+    };
+    // the stages of one merge with partners PER / 2, ..., 1 apart: within the thread
+    auto local_stages = [&](int size) {
 #pragma unroll
-    for (int ls = 1; ls <= LOG; ls++) {
-        const int size = 1 << ls;
+        for (int j = PER / 2; j > 0; j >>= 1) {
+            if (j < size) {
 #pragma unroll
-        for (int lj = ls - 1; lj >= 0; lj--) {
-            const int j = 1 << lj;
-            if (j < PER) {
+                for (int e = 0; e < PER; e++)
+                    if ((e & j) == 0) cx(e, e | j, size);
+            }
+        }
+    };
+    for (int size = 2; size <= CAP; size <<= 1) {
+        for (int j = size >> 1; j >= PER; j >>= 1) {  // partners in other threads
+            const bool cross = j >= 32 * PER;
+            if (cross) {
+                __syncthreads();  // the previous cross stage's readers are done
 #pragma unroll
                 for (int e = 0; e < PER; e++) {
-                    if ((e & j) == 0) {
-                        const int e2 = e | j;
-                        const bool asc = ((tid * PER + e) & size) == 0;
-                        if ((k[e] > k[e2]) == asc) {
-                            const u64 tk = k[e];
-                            k[e] = k[e2];
-                            k[e2] = tk;
-                            const int32_t tv = v[e];
-                            v[e] = v[e2];
-                            v[e2] = tv;
-                        }
-                    }
+                    sk[tid * PER + e] = k[e];
+                    ss[tid * PER + e] = v[e];
                 }
-            } else {
-                const bool cross = j >= 32 * PER;
+                __syncthreads();
+            }
+            const bool lower = ((tid * PER) & j) == 0;
+#pragma unroll
+            for (int e = 0; e < PER; e++) {
+                const bool asc = ((tid * PER + e) & size) == 0;
+                u64 ok;
+                int32_t ov;
                 if (cross) {
-                    __syncthreads();  // the previous cross stage's readers are done
-#pragma unroll
-                    for (int e = 0; e < PER; e++) {
-                        sk[tid * PER + e] = k[e];
-                        ss[tid * PER + e] = v[e];
-                    }
-                    __syncthreads();
+                    ok = sk[(tid * PER + e) ^ j];
+                    ov = ss[(tid * PER + e) ^ j];
+                } else {
+                    ok = __shfl_xor_sync(0xffffffffu, k[e], j / PER);
+                    ov = __shfl_xor_sync(0xffffffffu, v[e], j / PER);
                 }
-                const bool lower = ((tid * PER) & j) == 0;
-#pragma unroll
-                for (int e = 0; e < PER; e++) {
-                    const bool asc = ((tid * PER + e) & size) == 0;
-                    u64 ok;
-                    int32_t ov;
-                    if (cross) {
-                        ok = sk[(tid * PER + e) ^ j];
-                        ov = ss[(tid * PER + e) ^ j];
-                    } else {
-                        ok = __shfl_xor_sync(0xffffffffu, k[e], j / PER);
-                        ov = __shfl_xor_sync(0xffffffffu, v[e], j / PER);
-                    }
-                    const bool take = (lower == asc) ? ok < k[e] : ok > k[e];
-                    if (take) {
-                        k[e] = ok;
-                        v[e] = ov;
-                    }
+                const bool take = (lower == asc) ? ok < k[e] : ok > k[e];
+                if (take) {
+                    k[e] = ok;
+                    v[e] = ov;
                 }
             }
         }
+        local_stages(size);
     }
     __syncthreads();  // the last cross stage's readers are done
 #pragma unroll

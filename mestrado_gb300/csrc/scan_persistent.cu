@@ -582,8 +582,10 @@ constexpr int FIN_NT_BIG = 512;
 constexpr double MIX_DELTA = 0x1p-9;
 constexpr double MIX_EPS_REL = 0x1p-12;
 constexpr double MIX_EPS_ABS = 0x1p-12;
-// the precision form's final sort: keys per thread of the register bitonic network
+// the precision form's final sort: keys per thread of the register bitonic network, and the
+// largest second re-score round merged without a second select
 constexpr int FIN_SORT_PER = 8;
+constexpr int FIN_XTRA = 256;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -752,8 +754,9 @@ __global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 3) : 0) finalize_ker
         // candidates to re-score are gathered into a list (ids[], whose identity contents this form
         // does not need), and only the final kk exact keys are sorted, in registers.
         static_assert(NT == FIN_NT && NT * FIN_SORT_PER >= 1024, "the final sort holds kl <= 1024 keys");
-        u64* sk = reinterpret_cast<u64*>(xq + 128);              // the final sort's staging (d = 128)
-        int32_t* ss = reinterpret_cast<int32_t*>(sk + NT * FIN_SORT_PER);
+        // the final sort's staging (d = 128): keys, then slots, each for NT * FIN_SORT_PER + FIN_XTRA
+        u64* sk = reinterpret_cast<u64*>(xq + 128);
+        int32_t* ss = reinterpret_cast<int32_t*>(sk + NT * FIN_SORT_PER + FIN_XTRA);
         int32_t* list = ids;
         const int kk0 = (rerank || refine) ? a.kl : query_k(a, q);
         const int ksel = min(kk0 * a.sel_mult, a.sel_cap);
@@ -782,87 +785,164 @@ __global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 3) : 0) finalize_ker
             for (int c0 = tid & ~31; c0 < n; c0 += NT) {
                 const int c = c0 + lane;
                 const bool in = c < n && pred(c);
-                const unsigned m = __ballot_sync(0xffffffffu, in);
-                if (m == 0u) continue;
+                const unsigned mk = __ballot_sync(0xffffffffu, in);
+                if (mk == 0u) continue;
                 int base = 0;
                 if (lane == 0) {
-                    base = atomicAdd(&s_cnt, __popc(m));
-                    s_flag[c0 >> 5] |= m;
+                    base = atomicAdd(&s_cnt, __popc(mk));
+                    s_flag[c0 >> 5] |= mk;
                 }
                 base = __shfl_sync(0xffffffffu, base, 0);
-                if (in) list[base + __popc(m & ((1u << lane) - 1u))] = c;
+                if (in) list[base + __popc(mk & ((1u << lane) - 1u))] = c;
             }
-        };
-        auto rescore = [&](int c) {
-            keys[c] = make_key(exact_adc<M>(ix, xq, a.cand_list[hb + c], a.cand_id[hb + c]), key_payload(keys[c]));
-            return keys[c];
         };
         gather([&](int c) { return keys[c] <= th; });
         __syncthreads();
         const int m0 = s_cnt;
+        int m = m0;
+        // two rounds of exact re-scores (one copy of the loop): list[0 .. m0), then list[m0 .. m).
+        // Before each, one pass fetches the candidates' lists and code rows into meta[] (the final
+        // sort's staging, free until then) and asks L2 for their code rows and list centroids, so
+        // the re-score loop starts from on-chip data instead of three dependent memory round trips.
+        int2* meta = reinterpret_cast<int2*>(sk);  // NT * FIN_SORT_PER entries: (list, row)
+        constexpr int META = NT * FIN_SORT_PER;
         u64 t0 = 0;
-        for (int i = tid; i < m0; i += NT) {
-            const u64 key = rescore(list[i]);
-            t0 = key > t0 ? key : t0;
-        }
-        // the largest squared residual norm over the query's probes (a bound on ||r||^2 for every
-        // candidate, handed off or not)
-        float r2 = 0.0f;
-        for (int j = tid; j < query_w(a, q); j += NT) {
-            const int l = a.probes[(int64_t)q * a.w + j];
-            if (l < 0 || l >= ix.C) continue;
-            const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128);
-            float sq = 0.0f;
-#pragma unroll 8
-            for (int v = 0; v < 32; v++) {
-                const float4 y = __ldg(y4 + v);
-                const float d0 = xq[4 * v] - y.x, d1 = xq[4 * v + 1] - y.y, d2 = xq[4 * v + 2] - y.z,
-                            d3 = xq[4 * v + 3] - y.w;
-                sq = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, sq))));
+        for (int round = 0, i0 = 0; round < 2; round++) {
+            for (int i = i0 + tid; i < min(m, META); i += NT) {
+                const int c = list[i];
+                const int l = a.cand_list[hb + c], row = a.cand_id[hb + c];
+                meta[i] = make_int2(l, row);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(ix.codes + (int64_t)row * M)));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(ix.coa + (int64_t)l * 128)));
             }
-            r2 = fmaxf(r2, sq);
-        }
-        atomicMax(&s_t0, t0);
-        atomicMax(&s_r2, __float_as_uint(r2));  // (non-negative floats order as their bits)
-        __syncthreads();
-        const double T0 = fmax(0.0, (double)key_dist(s_t0));
-        const double eps = MIX_EPS_REL * ((double)__uint_as_float(s_r2) * (1.0 + 0x1p-10) + (double)ix.pq_cmax) +
-                           MIX_EPS_ABS;
-        const double tau = (T0 + eps) / (1.0 - MIX_DELTA) * (1.0 + 0x1p-20);
-        // the rest of the candidates below tau (their keys are still approximate)
-        gather([&](int c) { return !((s_flag[c >> 5] >> (c & 31)) & 1u) && (double)key_dist(keys[c]) < tau; });
-        __syncthreads();
-        const int m = s_cnt;
-        for (int i = m0 + tid; i < m; i += NT) rescore(list[i]);
-        // not proven: the hand-off is full (candidates may lie beyond it) and all of it is below tau
-        if (tid == 0 && a.unproven && n >= ksel && (double)key_dist(s_amax) < tau) atomicAdd(a.unproven, 1);
-        __syncthreads();
-        // the kk best exact keys of the re-scored set, in order
-        const u64 th2 = m > kk ? block_kth_flagged(keys, n, s_flag, kk) : KEY_MAX;
-        for (int c0 = tid & ~31; c0 < n; c0 += NT) {
-            const int c = c0 + lane;
-            const bool in = c < n && ((s_flag[c >> 5] >> (c & 31)) & 1u) && keys[c] <= th2;
-            const unsigned mk = __ballot_sync(0xffffffffu, in);
-            if (mk == 0u) continue;
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&s_cnt2, __popc(mk));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (in) {
-                const int o = base + __popc(mk & ((1u << lane) - 1u));
-                sk[o] = keys[c];
-                ss[o] = c;
+            __syncthreads();
+            for (int i = i0 + tid; i < m; i += NT) {
+                const int c = list[i];
+                const int2 lr = i < META ? meta[i] : make_int2(a.cand_list[hb + c], a.cand_id[hb + c]);
+                const u64 key = make_key(exact_adc<M>(ix, xq, lr.x, lr.y), key_payload(keys[c]));
+                keys[c] = key;
+                t0 = key > t0 ? key : t0;
             }
+            if (round == 1) break;
+            // the largest squared residual norm over the query's probes (a bound on ||r||^2 for
+            // every candidate, handed off or not): four threads per probe, 32 dimensions each
+            float r2 = 0.0f;
+            const int wq = query_w(a, q);
+            for (int j0 = 0; j0 < wq; j0 += NT / 4) {  // block-uniform trip count (shuffles below)
+                const int j = j0 + tid / 4, part = tid & 3;
+                float sq = 0.0f;
+                const int l = j < wq ? a.probes[(int64_t)q * a.w + j] : -1;
+                if (l >= 0 && l < ix.C) {
+                    const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128 + 32 * part);
+                    const float* xp = xq + 32 * part;
+                    float4 y[8];
+#pragma unroll
+                    for (int v = 0; v < 8; v++) y[v] = __ldg(y4 + v);
+#pragma unroll
+                    for (int v = 0; v < 8; v++) {
+                        const float d0 = xp[4 * v] - y[v].x, d1 = xp[4 * v + 1] - y[v].y, d2 = xp[4 * v + 2] - y[v].z,
+                                    d3 = xp[4 * v + 3] - y[v].w;
+                        sq = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, sq))));
+                    }
+                }
+                sq += __shfl_xor_sync(0xffffffffu, sq, 1);
+                sq += __shfl_xor_sync(0xffffffffu, sq, 2);
+                r2 = fmaxf(r2, sq);
+            }
+            atomicMax(&s_t0, t0);
+            atomicMax(&s_r2, __float_as_uint(r2));  // (non-negative floats order as their bits)
+            __syncthreads();
+            const double T0 = fmax(0.0, (double)key_dist(s_t0));
+            const double eps = MIX_EPS_REL * ((double)__uint_as_float(s_r2) * (1.0 + 0x1p-10) + (double)ix.pq_cmax) +
+                               MIX_EPS_ABS;
+            const double tau = (T0 + eps) / (1.0 - MIX_DELTA) * (1.0 + 0x1p-20);
+            // the rest of the candidates below tau (their keys are still approximate)
+            gather([&](int c) { return !((s_flag[c >> 5] >> (c & 31)) & 1u) && (double)key_dist(keys[c]) < tau; });
+            // not proven: the hand-off is full (candidates may lie beyond it) and all of it is below tau
+            if (tid == 0 && a.unproven && n >= ksel && (double)key_dist(s_amax) < tau) atomicAdd(a.unproven, 1);
+            __syncthreads();
+            i0 = m0;
+            m = s_cnt;
         }
         __syncthreads();
-        const int nout = s_cnt2;  // min(m, kk): the keys are unique
-        if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
-        else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, nout);
-        for (int c = tid; c < nout; c += NT) {
-            keys[c] = sk[c];
-            ids[c] = ss[c];
+        // The kk best exact keys of the re-scored set, in order. The first round's set holds
+        // min(n, kk) keys and the second round usually adds a few: both are sorted (the first in
+        // registers, the second by rank) and merged, each key's place being its rank in its own set
+        // plus the number of smaller keys in the other. A large second set goes through a radix
+        // select of the kk-th key and one sort instead.
+        u64* xk = sk + META;                                   // second set: FIN_XTRA keys ...
+        int32_t* xs = reinterpret_cast<int32_t*>(ss + META);   // ... and slots
+        const int m1 = m - m0;
+        if (m1 <= FIN_XTRA) {
+            for (int i = tid; i < m0; i += NT) {
+                sk[i] = keys[list[i]];
+                ss[i] = list[i];
+            }
+            for (int i = tid; i < m1; i += NT) {
+                xk[i] = keys[list[m0 + i]];
+                xs[i] = list[m0 + i];
+            }
+            __syncthreads();
+            if (m0 <= RANK_SORT_MAX) rank_sort(sk, ss, m0);
+            else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, m0);
+            if (m1 > 1) rank_sort(xk, xs, m1);
+            // (both sorts end with a barrier)
+            const int nout = min(m, kk0);
+            for (int i = tid; i < m0; i += NT) {
+                const u64 key = sk[i];
+                int lo = 0, hi = m1;  // smaller keys of the second set
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (xk[mid] < key) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (i + lo < nout) {
+                    keys[i + lo] = key;
+                    ids[i + lo] = ss[i];
+                }
+            }
+            for (int i = tid; i < m1; i += NT) {
+                const u64 key = xk[i];
+                int lo = 0, hi = m0;  // smaller keys of the first set
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (sk[mid] < key) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (i + lo < nout) {
+                    keys[i + lo] = key;
+                    ids[i + lo] = xs[i];
+                }
+            }
+            __syncthreads();
+            n = nout;
+        } else {
+            const u64 th2 = m > kk ? block_kth_flagged(keys, n, s_flag, kk) : KEY_MAX;
+            for (int c0 = tid & ~31; c0 < n; c0 += NT) {
+                const int c = c0 + lane;
+                const bool in = c < n && ((s_flag[c >> 5] >> (c & 31)) & 1u) && keys[c] <= th2;
+                const unsigned mk = __ballot_sync(0xffffffffu, in);
+                if (mk == 0u) continue;
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_cnt2, __popc(mk));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (in) {
+                    const int o = base + __popc(mk & ((1u << lane) - 1u));
+                    sk[o] = keys[c];
+                    ss[o] = c;
+                }
+            }
+            __syncthreads();
+            const int nout = s_cnt2;  // min(m, kk): the keys are unique
+            if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
+            else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, nout);
+            for (int c = tid; c < nout; c += NT) {
+                keys[c] = sk[c];
+                ids[c] = ss[c];
+            }
+            __syncthreads();
+            n = nout;
         }
-        __syncthreads();
-        n = nout;
     } else {
         if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);
         else bitonic_sort_pairs(keys, ids, p2);
@@ -951,7 +1031,8 @@ int scan_persistent_stride(const ScanArgs& a) {
 template <int M, bool MIXED>
 static cudaError_t launch_fin(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
     // keys, ids, the query; the precision form's final sort staging
-    const size_t fsm = (size_t)a.cand_stride * 12 + 512 + (MIXED ? (size_t)FIN_NT * FIN_SORT_PER * 12 : 0);
+    const size_t fsm =
+        (size_t)a.cand_stride * 12 + 512 + (MIXED ? (size_t)(FIN_NT * FIN_SORT_PER + FIN_XTRA) * 12 : 0);
     const bool big = !MIXED && (a.flags & SCAN_REFINE);
     void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
     if constexpr (!MIXED)

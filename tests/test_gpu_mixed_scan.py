@@ -145,7 +145,7 @@ def test_mixed_scan_long_lists_every_shape(long_list_indexes, m, threads, monkey
     monkeypatch.setenv("GBIVF_SCAN_THREADS", threads)
     ixs, q = long_list_indexes
     gi = GpuIndex(ixs[m])
-    for k, w in ((10, 3), (100, 8)):
+    for k, w in ((10, 3), (100, 8), (1000, 8)):  # (k = 1000 at m = 4: a wide second re-score round)
         a = gi.search(q, k, w)
         b = gi.search(q, k, w, mixed_scan=True)
         u = gi.last_unproven()
