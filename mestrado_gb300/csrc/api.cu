@@ -565,7 +565,8 @@ int make_query_tiles(gbivf_index* ix, const float* qb, int nb, cudaStream_t st) 
 
 // Filtered coarse stage (coarse_filter.cu) for large C, plain or mixed form.
 int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, int nq, int w, bool mixed, int S,
-                          int r, int cap, int32_t* coaidx, float* coadis, int* fl, cudaStream_t st) {
+                          int r, int cap, int32_t* coaidx, float* coadis, int* fl, cudaStream_t st,
+                          const int32_t* d_w) {
     const DevIndex& dx = ix->dx;
     // queries per block: the sample block (bq x S floats) within 256 Mi floats
     int64_t bq = std::min<int64_t>(nq, std::max<int64_t>(MMA_QUERY_TILE, (256ll << 20) / S));
@@ -612,6 +613,12 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
         const int nb = (int)std::min<int64_t>(bq, nq - q0);
         const float* qb = d_q + q0 * dx.d;
         CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(int) * (size_t)bq, st));
+        // an uneven batch: each query's bound, candidates and selection for its own probe count
+        SampleRank sr;
+        sr.w_per_q = d_w ? d_w + q0 : nullptr;
+        sr.w = w;
+        sr.scale = 2.0 * S / (double)dx.C;
+        f.w_per_q = sr.w_per_q;
         if (mixed) {
             uint8_t* qt = ix->w_qtiles.as<uint8_t>();
             int rc = make_query_tiles(ix, qb, nb, st);
@@ -622,11 +629,11 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
                 // sample: minima of 32-centroid chunks straight from the GEMM, bound from those
                 CK(launch_coarse_gemm_chunkmin(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, colG,
                                                colK, cd, S / 32, ix->num_sms, fl, st));
-                CK(launch_coarse_sample_bound(cd, nb, S / 32, S / 32, r, thr, st));
+                CK(launch_coarse_sample_bound(cd, nb, S / 32, S / 32, r, thr, st, sr));
             } else {
                 CK(launch_coarse_gemm_store(qt, ix->coa_tiles.as<uint8_t>(), nb, S, qn + q0, dx.coa_norm, cd, S,
                                             ix->num_sms, fl, st));
-                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, dx.coa_norm, ix->coa_len.as<float>(), thr, st));
+                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, dx.coa_norm, ix->coa_len.as<float>(), thr, st, sr));
             }
             surv_shape(nb, &f.nsplit, &f.sreg);
             f.surv = ix->w_surv.as<int2>();
@@ -636,9 +643,9 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
         } else {
             CK(launch_coarse_dist(sx, qb, qn + q0, nb, cd, st));
             if (r <= 128)
-                CK(launch_coarse_sample_bound(cd, nb, S, S, r, thr, st));
+                CK(launch_coarse_sample_bound(cd, nb, S, S, r, thr, st, sr));
             else
-                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, nullptr, nullptr, thr, st));
+                CK(launch_coarse_sample_kth(cd, nb, S, r, qn + q0, nullptr, nullptr, thr, st, sr));
             CK(launch_coarse_dist_filter(dx, qb, qn + q0, nb, f, st));
         }
         CK(launch_coarse_cand_select(dx, qb, qn + q0, nb, w, f, coaidx + q0 * w, coadis + q0 * w, fl + 1, st));
@@ -646,11 +653,13 @@ int coarse_stage_filtered(gbivf_index* ix, const float* d_q, const double* qn, i
     return GBIVF_OK;
 }
 
-// Coarse stage: coaidx/coadis (nq x w) for device queries d_q with norms qn.
+// Coarse stage: coaidx/coadis (nq x w) for device queries d_q with norms qn; with d_w (an uneven
+// batch) the large-C filtered stage selects only each query's first d_w[q] entries (the rest of the
+// row is -1), the prefix of its top-w.
 // The flags word w_flags holds [0] the device error flag, [1] the number of
 // centroids re-checked exactly, [2] the queries that took all C centroids.
 int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, int w, unsigned flags, int32_t* coaidx,
-                 float* coadis, cudaStream_t st) {
+                 float* coadis, cudaStream_t st, const int32_t* d_w = nullptr) {
     const DevIndex& dx = ix->dx;
     if (dx.C == 1) {
         CK(cudaMemsetAsync(coaidx, 0, sizeof(int32_t) * nq, st));
@@ -666,7 +675,7 @@ int coarse_stage(gbivf_index* ix, const float* d_q, const double* qn, int nq, in
         CK(ix->w_flags.ensure(4 * sizeof(int)));
         CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
         int rc = coarse_stage_filtered(ix, d_q, qn, nq, w, mixed, S, r, cap, coaidx, coadis, ix->w_flags.as<int>(),
-                                       st);
+                                       st, d_w);
         if (rc) return rc;
         ix->mixed_pending = true;
         return GBIVF_OK;
@@ -762,7 +771,7 @@ int search_device_impl(gbivf_index* ix, const float* d_q, int nq, int k, int kl,
     CK(cudaMemsetAsync(ix->w_flags.p, 0, 4 * sizeof(int), st));
     CK(launch_norm_d(d_q, nq, dx.d, qn, st));
     {
-        int rc = coarse_stage(ix, d_q, qn, nq, w, flags, coaidx, coadis, st);
+        int rc = coarse_stage(ix, d_q, qn, nq, w, flags, coaidx, coadis, st, d_w);
         if (rc) return rc;
     }
     ScanArgs a;

@@ -63,12 +63,20 @@ bool coarse_filter_shape(int C, int w, int d, int* S, int* r, int* cap) {
     return true;
 }
 
-// thr[q] = r-th smallest of row q (plus mixed_eps when clen != NULL)
+// the sample rank of a query that takes wq of the batch's w probes: the batch's rank r scaled down
+// (about twice the centroids the query needs below its bound), never above r
+__device__ __forceinline__ int sample_rank(const SampleRank& sr, int r, int q) {
+    if (!sr.w_per_q) return r;
+    const int wq = min(max(sr.w_per_q[q], 1), sr.w);
+    return max(1, min(r, (int)ceil(sr.scale * wq) + 8));
+}
+
+// thr[q] = r_q-th smallest of row q (plus mixed_eps when clen != NULL)
 __global__ void __launch_bounds__(KT_NT) coarse_sample_kth_kernel(const float* __restrict__ vals, int S, int r,
                                                                   const double* __restrict__ qnorm,
                                                                   const float* __restrict__ cnorm,
                                                                   const float* __restrict__ clen, int kcap, int bcap,
-                                                                  float* __restrict__ thr) {
+                                                                  SampleRank sr, float* __restrict__ thr) {
     extern __shared__ __align__(16) unsigned char smem[];
     u64* best = reinterpret_cast<u64*>(smem);
     u64* tmp = best + kcap;
@@ -94,11 +102,12 @@ __global__ void __launch_bounds__(KT_NT) coarse_sample_kth_kernel(const float* _
         topk_round_end(s, KT_NT * KT_ITEMS);
     }
     topk_finish(s);
-    if (tid == 0) thr[q] = key_dist(best[min(r, *s.nbest) - 1]);
+    if (tid == 0) thr[q] = key_dist(best[min(sample_rank(sr, r, q), *s.nbest) - 1]);
 }
 
 cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, const double* qnorm,
-                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st) {
+                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st,
+                                     SampleRank sr) {
     if (nq <= 0) return cudaSuccess;
     if (r < 1 || r > S) return cudaErrorInvalidValue;
     const int kcap = pow2_ge(std::max(r, 2));
@@ -109,15 +118,15 @@ cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, co
             cudaFuncSetAttribute(coarse_sample_kth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    coarse_sample_kth_kernel<<<nq, KT_NT, sm, st>>>(vals, S, r, qnorm, cnorm, clen, kcap, bcap, thr);
+    coarse_sample_kth_kernel<<<nq, KT_NT, sm, st>>>(vals, S, r, qnorm, cnorm, clen, kcap, bcap, sr, thr);
     return cudaGetLastError();
 }
 
 constexpr int KB_NT = 512;  // sample bound: groups per query
 
-// thr[q] = r-th smallest of the minima of KB_NT interleaved groups of row q
+// thr[q] = r_q-th smallest of the minima of KB_NT interleaved groups of row q
 __global__ void __launch_bounds__(KB_NT) coarse_sample_bound_kernel(const float* __restrict__ vals, int L, int64_t ld,
-                                                                    int r, float* __restrict__ thr) {
+                                                                    int r, SampleRank sr, float* __restrict__ thr) {
     __shared__ u64 keys[KB_NT];
     __shared__ __align__(8) unsigned char work[TOPK_WORK_BYTES];
     const int q = blockIdx.x, tid = threadIdx.x;
@@ -129,15 +138,15 @@ __global__ void __launch_bounds__(KB_NT) coarse_sample_bound_kernel(const float*
     TopKSmem s{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, r, 0, 0, work};
     if (tid == 0) s.slots()[0] = 0;
     __syncthreads();
-    const u64 kth = block_kth(s, keys, KB_NT, keys, 0, r);
+    const u64 kth = block_kth(s, keys, KB_NT, keys, 0, sample_rank(sr, r, q));
     if (tid == 0) thr[q] = key_dist(kth);
 }
 
 cudaError_t launch_coarse_sample_bound(const float* vals, int nq, int L, int64_t ld, int r, float* thr,
-                                       cudaStream_t st) {
+                                       cudaStream_t st, SampleRank sr) {
     if (nq <= 0) return cudaSuccess;
     if (r < 1 || r > KB_NT / 4 || r > L || ld < L) return cudaErrorInvalidValue;
-    coarse_sample_bound_kernel<<<nq, KB_NT, 0, st>>>(vals, L, ld, r, thr);
+    coarse_sample_bound_kernel<<<nq, KB_NT, 0, st>>>(vals, L, ld, r, sr, thr);
     return cudaGetLastError();
 }
 
@@ -214,10 +223,12 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
         n = f.ncand[q];
         below = f.cnt ? f.cnt[q] : n;
     }
-    const bool all = overflow || n > f.cap || below < w;
+    // the query's own probe count (an uneven batch): its top-wq is the prefix of its top-w
+    const int wq = f.w_per_q ? min(max(f.w_per_q[q], 1), w) : w;
+    const bool all = overflow || n > f.cap || below < wq;
     const int total = all ? C : n;  // without the fallback n <= cap <= bcap: no flush until the end
     const int32_t* cq = f.cand + (int64_t)q * f.cap;
-    topk_init(s, w);  // (its barrier also publishes xq)
+    topk_init(s, wq);  // (its barrier also publishes xq)
     for (int i0 = 0; i0 < total; i0 += CC_NT) {
         const int i = i0 + tid;
         const bool valid = i < total;
@@ -250,7 +261,7 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
         if (all) topk_round_end(s, CC_NT);
     }
     topk_finish(s);
-    const int nb = *s.nbest;
+    const int nb = min(*s.nbest, wq);
     for (int j = tid; j < w; j += CC_NT) {
         coaidx[(int64_t)q * w + j] = j < nb ? (int32_t)key_payload(best[j]) : -1;
         coadis[(int64_t)q * w + j] = j < nb ? key_dist(best[j]) : __int_as_float(0x7f800000);

@@ -198,6 +198,16 @@ struct CoarseFilter {
     int2* surv = nullptr;
     int* scnt = nullptr;
     int sreg = 0, nsplit = 0;
+    // uneven batches: each query's probe count (<= w; NULL: w for all), so that its candidates and
+    // selection cover its own top-wq only
+    const int32_t* w_per_q = nullptr;
+};
+// the sample rank of each query of an uneven batch: min(r, ceil(scale * wq) + 8), wq = the query's
+// probe count clamped to 1..w (w_per_q NULL: r for all)
+struct SampleRank {
+    const int32_t* w_per_q = nullptr;
+    int w = 0;
+    double scale = 0.0;
 };
 // sample size, rank and candidate capacity of the filtered stage; false when
 // the plain select over the full distance block is used instead
@@ -242,11 +252,12 @@ cudaError_t launch_coarse_gemm_filter(const uint8_t* qtiles, const uint8_t* ctil
 // stride ld): the r-th smallest of the minima of 512 interleaved groups (so
 // at least r values lie at or below it); r <= 128 and r <= L
 cudaError_t launch_coarse_sample_bound(const float* vals, int nq, int L, int64_t ld, int r, float* thr,
-                                       cudaStream_t st);
+                                       cudaStream_t st, SampleRank sr = SampleRank());
 // thr[q] = r-th smallest of a nq x S block of distances (clen != NULL: of the
 // upper bounds approx + mixed_eps)
 cudaError_t launch_coarse_sample_kth(const float* vals, int nq, int S, int r, const double* qnorm,
-                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st);
+                                     const float* cnorm, const float* clen, float* thr, cudaStream_t st,
+                                     SampleRank sr = SampleRank());
 // exact keyed top-w per query from the candidates of f (stats[0] += candidates
 // re-checked, stats[1] += queries that fell back to all C centroids)
 cudaError_t launch_coarse_cand_select(const DevIndex& ix, const float* q, const double* qnorm, int nq, int w,
