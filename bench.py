@@ -46,6 +46,7 @@ import argparse
 import hashlib
 import json
 import math
+import re
 import os
 import statistics
 import subprocess
@@ -359,6 +360,18 @@ def cpu_batched(ix, q, wq, kq, nthreads):
 
 def sample_size(seconds_per_query, target_s, lo, hi):
     return int(max(lo, min(hi, target_s / max(seconds_per_query, 1e-9))))
+
+
+def mixed_alpha():
+    """The precision form's approximate selection, max(alpha * k, k + extra): (alpha, extra) from the
+    header's GBIVF_MIXED_SCAN_ALPHA and GBIVF_MIXED_SCAN_EXTRA, alpha overridden by the
+    GBIVF_MIXED_SCAN_SEL variable the engine reads."""
+    hdr = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "include", "gbivf.h")).read()
+    alpha = int(re.search(r"#define GBIVF_MIXED_SCAN_ALPHA (\d+)", hdr).group(1))
+    extra = int(re.search(r"#define GBIVF_MIXED_SCAN_EXTRA (\d+)", hdr).group(1))
+    if os.environ.get("GBIVF_MIXED_SCAN_SEL"):
+        alpha = min(16, max(1, int(os.environ["GBIVF_MIXED_SCAN_SEL"])))
+    return alpha, extra
 
 
 def core_cpu_baseline(ix, queries, c):
@@ -757,7 +770,9 @@ def large_record(args, name, c, dev, rank, world, dist, local_rank, headline):
     # algorithmic bytes are the codes of the probes the first pass left to it (the engine's rule: each
     # query's leading probes up to beta * k_sel rows go to the first pass); else the per-query scan kernel.
     if mx["scan_counters"]["list_scan"]:
-        sel = np.minimum(kq.astype(np.int64) * 4, 4096)  # the precision form's k_sel
+        alpha, extra = mixed_alpha()
+        kq64 = kq.astype(np.int64)
+        sel = np.minimum(np.maximum(kq64 * alpha, kq64 + extra), 4096)  # the precision form's k_sel
         rows = np.where(probed >= 0, sizes[np.maximum(probed, 0)], 0)
         csum = np.cumsum(rows, axis=1)
         lead = (csum < sel[:, None]).sum(1) + 1  # leading probes holding beta * k_sel rows (beta = 1)

@@ -47,13 +47,15 @@ extern "C" {
                                    the results are the same either way */
 #define GBIVF_MIXED_SCAN 0x10u  /* precision form of the scan (d = 128, ks = 256, m in {4, 8, 16}): PQ tables
                                    built approximately (packed fused multiply-adds) and held in FP16,
-                                   summed in FP32; of the GBIVF_MIXED_SCAN_ALPHA * k best (at most 4096),
+                                   summed in FP32; of the max(GBIVF_MIXED_SCAN_ALPHA * k, k +
+                                   GBIVF_MIXED_SCAN_EXTRA) best (at most 4096),
                                    those within the tables' error bound of the k-th exact distance are
                                    re-scored in the reference's FP32 arithmetic, so every returned distance
                                    is the plain form's and the ids match it unless a true neighbour fell
                                    outside the approximate selection (gbivf_last_unproven counts the
                                    queries where that could not be excluded) */
-#define GBIVF_MIXED_SCAN_ALPHA 4
+#define GBIVF_MIXED_SCAN_ALPHA 2
+#define GBIVF_MIXED_SCAN_EXTRA 64 /* the approximate selection is at least k + GBIVF_MIXED_SCAN_EXTRA */
 #define GBIVF_RERANK_REFINE 0x20u /* re-rank the kl ADC candidates by the distance to their refined
                                      reconstruction y + c1(codes) + c2(refinement codes) instead of the
                                      raw vectors (needs gbivf_index_set_refine; k <= kl <= 1024). FP32:

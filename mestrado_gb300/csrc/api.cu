@@ -147,6 +147,7 @@ struct gbivf_index {
     int list_pref = -1;
     double mean_len = 0.0;
     int lc_ecap = 0;                  // per-query emission capacity of the list-centric scan (0: the default)
+    int sel_mult = GBIVF_MIXED_SCAN_ALPHA;  // the precision form's approximate selection per result
     // stage events (GBIVF_PROFILE): start, coarse done, search done, scan kernel done
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_valid = false;
@@ -280,6 +281,8 @@ int create_impl(gbivf_index** out, int device, int d, int coarsek, const float* 
     if (const char* v = getenv("GBIVF_LIST_SCAN_CAP")) ix->lc_ecap = std::max(0, atoi(v));
     // rows of the first pass per selected candidate (its threshold tightens as it grows)
     if (const char* v = getenv("GBIVF_LIST_SCAN_BETA")) ix->lcw.beta = std::max(1, atoi(v));
+    // the precision form's approximate selection, GBIVF_MIXED_SCAN_ALPHA * k by default
+    if (const char* v = getenv("GBIVF_MIXED_SCAN_SEL")) ix->sel_mult = std::min(16, std::max(1, atoi(v)));
     if (const char* v = getenv("GBIVF_SCAN_KERNEL")) {
         ix->use_persistent = strcmp(v, "general") != 0;
         ix->list_mode = strcmp(v, "lists") == 0 ? 1 : 2;
@@ -427,7 +430,8 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
     const bool mixed = a.flags & SCAN_MIXED;
     ix->last_mixed = mixed;
     if (mixed) {
-        a.sel_mult = GBIVF_MIXED_SCAN_ALPHA;
+        a.sel_mult = ix->sel_mult;
+        a.sel_extra = GBIVF_MIXED_SCAN_EXTRA;
         a.sel_cap = 4096;
         if (!scan_persistent_supported(ix->dx, a))
             return fail(GBIVF_ERR_UNSUPPORTED, "GBIVF_MIXED_SCAN needs d = 128, ks = 256, m in {4, 8, 16} and "

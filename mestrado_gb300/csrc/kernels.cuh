@@ -69,6 +69,7 @@ struct ScanArgs {
     // precision form (SCAN_MIXED): the approximate selection size min(sel_mult * k, sel_cap), and
     // the hand-off's list of each candidate (cand_id then holds its code row)
     int sel_mult = 1, sel_cap = 0;
+    int sel_extra = 0;  // ... and at least k + sel_extra (mixed_sel)
     int32_t* cand_list = nullptr;
     // persistent scan over a subset of the batch: queries qlist[0 .. *nqlist) (NULL: 0 .. nq-1)
     const int32_t* qlist = nullptr;
@@ -79,6 +80,13 @@ struct ScanArgs {
     // to the exact form's (NULL: not counted)
     int* unproven = nullptr;
 };
+
+// the precision form's approximate selection for a query returning kk results:
+// min(max(sel_mult * kk, kk + sel_extra), sel_cap)
+__host__ __device__ __forceinline__ int mixed_sel(const ScanArgs& a, int kk) {
+    const int s = a.sel_mult * kk > kk + a.sel_extra ? a.sel_mult * kk : kk + a.sel_extra;
+    return s < a.sel_cap ? s : a.sel_cap;
+}
 
 // per-query shape of a (possibly uneven) batch
 // (values outside 1..w / 1..k are clamped, so a bad entry cannot overrun buffers)

@@ -58,7 +58,7 @@ struct LcShape {
 
 __device__ __forceinline__ int lc_ksel(const ScanArgs& a, int q) {
     const int kq0 = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : query_k(a, q);
-    return (a.flags & SCAN_MIXED) ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
+    return (a.flags & SCAN_MIXED) ? mixed_sel(a, kq0) : kq0;
 }
 
 // ---------------------------------------------------------------------------

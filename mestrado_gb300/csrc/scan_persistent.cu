@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(NT, 1) ivf_scan_persistent_kernel(DevIndex ix,
         if (tid == 0) qslot[1] = atomicAdd(a.queue, 1);  // next query, in flight meanwhile
         const int kq0 = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : query_k(a, q);
         // the precision form keeps alpha * k approximate candidates for the exact re-score
-        const int kq = MIXED ? min(kq0 * a.sel_mult, a.sel_cap) : kq0;
+        const int kq = MIXED ? mixed_sel(a, kq0) : kq0;
         // prefix sums of the probe lengths (each lane reads, then overwrites, its own slot)
         if (tid < 32) {
             uint32_t carry = 0;
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 3) : 0) finalize_ker
         int32_t* ss = reinterpret_cast<int32_t*>(sk + NT * FIN_SORT_PER + FIN_XTRA);
         int32_t* list = ids;
         const int kk0 = (rerank || refine) ? a.kl : query_k(a, q);
-        const int ksel = min(kk0 * a.sel_mult, a.sel_cap);
+        const int ksel = mixed_sel(a, kk0);
         const int kk = min(n, kk0);
         const int lane = tid & 31;
         __shared__ unsigned s_flag[4096 / 32];  // bit c: candidate c re-scored (n <= sel_cap <= 4096)
@@ -1024,7 +1024,7 @@ bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
 
 int scan_persistent_stride(const ScanArgs& a) {
     const int kk = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : a.k;
-    const int sel = (a.flags & SCAN_MIXED) ? std::min(kk * a.sel_mult, a.sel_cap) : kk;
+    const int sel = (a.flags & SCAN_MIXED) ? mixed_sel(a, kk) : kk;
     return pow2_at_least(std::max(std::max(sel, a.k), 2));
 }
 
