@@ -46,7 +46,7 @@
 namespace gbivf {
 
 constexpr int LC_NT = 512;        // threads of the list-centric scan (one CTA per SM)
-constexpr int LC_TILE = 16384;    // bytes of code rows per staged tile
+constexpr int LC_TILE = 32768;    // bytes of code rows per staged tile
 constexpr int LC_SEL_NT = 256;    // threads of the select kernel (one CTA per query)
 constexpr int LC_SEL_STAGE = 3072;  // keys of a query's pool the select kernel stages in shared memory
 constexpr int LC_HIST_SHIFT = 15;   // histogram bucket width: 2^15 float ulps below the first bound
@@ -577,22 +577,19 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
             const uint4* sg = stage + st * TILE_GROUPS;
             const int row0 = t * TILE_ROWS;
             const int ngt = min(TILE_GROUPS, (min(TILE_ROWS, len - row0) * M + 15) / 16);
-            uint4 cg[UG];
-#pragma unroll
-            for (int u = 0; u < UG; u++) {
-                const int gl = u * NT + tid;
-                cg[u] = gl < ngt ? sg[gl] : make_uint4(0, 0, 0, 0);
-            }
-#pragma unroll
+#pragma unroll 1
             for (int r0 = 0; r0 < RS; r0 += RB) {
                 if ((r0 / GR) * NT + (tid & ~31) >= ngt) break;  // warp-uniform: no rows left for this warp
-                // rows r0 .. r0 + RB - 1 of this thread: row slot r is row r % GR of group u = r / GR
+                // rows r0 .. r0 + RB - 1 of this thread: row slot r is row r % GR of group u = r / GR, read
+                // from the stage here (only the groups of this batch are held in registers)
                 float acc[RB][G];
                 int rowv[RB];
+                uint4 cb[RB];
 #pragma unroll
                 for (int rb = 0; rb < RB; rb++) {
-                    const int r = r0 + rb;
-                    rowv[rb] = row0 + ((r / GR) * NT + tid) * GR + r % GR;
+                    const int r = r0 + rb, gl = (r / GR) * NT + tid;
+                    rowv[rb] = row0 + gl * GR + r % GR;
+                    cb[rb] = gl < ngt ? sg[gl] : make_uint4(0, 0, 0, 0);
                 }
                 if constexpr (MIXED) {
                     // row-rotated order (rot_codes.cuh): the lanes of a quarter-warp, consecutive rows, read
@@ -604,7 +601,7 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
 #pragma unroll
                         for (int g = 0; g < G; g++) s8[rb][g] = 0.0f;
                         const int r = r0 + rb, rr = r % GR;
-                        const uint4 c = cg[r / GR];
+                        const uint4 c = cb[rb];
                         const int rot = row_rot<M>(rowv[rb]);
                         if constexpr (M == 16) {
                             rc[rb] = rot_bytes(c, rot);
@@ -639,8 +636,8 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
                     for (int s = 0; s < M; s++) {
 #pragma unroll
                         for (int rb = 0; rb < RB; rb++) {
-                            const int r = r0 + rb, u = r / GR, rr = r % GR;
-                            const uint4 c = cg[u];
+                            const int rr = (r0 + rb) % GR;
+                            const uint4 c = cb[rb];
                             const uint32_t cw = (rr * M + s) >> 2 == 0 ? c.x
                                               : (rr * M + s) >> 2 == 1 ? c.y
                                               : (rr * M + s) >> 2 == 2 ? c.z : c.w;
