@@ -46,7 +46,7 @@
 namespace gbivf {
 
 constexpr int LC_NT = 512;        // threads of the list-centric scan (one CTA per SM)
-constexpr int LC_TILE = 32768;    // bytes of code rows per staged tile
+constexpr int LC_TILE = 65536;    // bytes of code rows per staged tile
 constexpr int LC_SEL_NT = 256;    // threads of the select kernel (one CTA per query)
 constexpr int LC_SEL_STAGE = 3072;  // keys of a query's pool the select kernel stages in shared memory
 constexpr int LC_HIST_SHIFT = 15;   // histogram bucket width: 2^15 float ulps below the first bound
@@ -314,6 +314,7 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
     float* ys = xs + 2 * G * D;                                 // [2][D]: their list centroids
     float* rr = ys + 2 * D;                                     // [G][D]: this item's residuals
     int4* desc = reinterpret_cast<int4*>(rr + G * D);           // [2][1 + G]: this item's descriptor and the next
+    float* rn = reinterpret_cast<float*>(desc + 2 * (1 + G));    // [G][M]: this item's residual sub-norms
     __shared__ __align__(16) u64 s_taup[2 * G];  // per slot the 16-byte pair of bounds holding its query's
     __shared__ u64 s_tau[G];                       // per slot its query's bound
     __shared__ int s_abort;
@@ -427,9 +428,20 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
             if (it + istep < nitems) fetch_desc(b ^ 1, it + istep);
             else lc_cp_async_commit();
         }
-        // residuals r = x_q - y_l (bsxfunMINUS, ivf_search.cpp:155-172)
-        for (int e = tid; e < G * D; e += NT)
-            rr[e] = e / D < np ? __fsub_rn(xs[b * G * D + e], ys[b * D + (e % D)]) : 0.0f;
+        // residuals r = x_q - y_l (bsxfunMINUS, ivf_search.cpp:155-172) and their sub-norms ||r_s||^2 in
+        // the reference's float order (nn.c:129-135): one thread per (query, sub-quantizer), once per
+        // item instead of once per table thread
+        if (tid < G * M) {
+            const int g = tid / M, sq = tid % M;
+            float r[DS];
+#pragma unroll
+            for (int t = 0; t < DS; t++)
+                r[t] = g < np ? __fsub_rn(xs[(b * G + g) * D + sq * DS + t], ys[b * D + sq * DS + t]) : 0.0f;
+#pragma unroll
+            for (int t = 0; t < DS; t += 4)
+                *reinterpret_cast<float4*>(rr + g * D + sq * DS + t) = make_float4(r[t], r[t + 1], r[t + 2], r[t + 3]);
+            rn[tid] = norm_f_seq(r, DS);
+        }
         __syncthreads();
         // the G interleaved tables from the register codebook
         if constexpr (MIXED) {
@@ -451,7 +463,7 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
                     f2_t rs2[DS];
 #pragma unroll
                     for (int t = 0; t < DS; t++) rs2[t] = f2_pack(rs[t], rs[t]);
-                    const float f4 = 0.25f * norm_f_seq(rs, DS);
+                    const float f4 = 0.25f * rn[g * M + my_s];
                     const f2_t f42 = f2_pack(f4, f4), mh2 = f2_pack(-0.5f, -0.5f);
 #pragma unroll
                     for (int p = 0; p < EM; p++) {
@@ -488,7 +500,7 @@ __global__ void __launch_bounds__(LC_NT, 1) lc_scan_kernel(DevIndex ix, ScanArgs
             const f2_t m2 = f2_pack(-2.0f, -2.0f), nz2 = f2_pack(a.neg_zero, a.neg_zero);
             float fq[G];
 #pragma unroll
-            for (int g = 0; g < G; g++) fq[g] = g < np ? norm_f_seq(rr + g * D + my_s * DS, DS) : 0.0f;
+            for (int g = 0; g < G; g++) fq[g] = g < np ? rn[g * M + my_s] : 0.0f;
 #pragma unroll
             for (int i = 0; i < E; i += 2) {
                 float o0[G], o1[G];
@@ -858,7 +870,7 @@ static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListSc
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = rec(2)) != cudaSuccess) return e;
     const size_t smem = 2 * LC_TILE + (size_t)M * 256 * 16 + sizeof(float) * (3 * G * 128 + 2 * 128) +
-                        sizeof(int4) * 2 * (1 + G);
+                        sizeof(int4) * 2 * (1 + G) + sizeof(float) * G * M;
     auto kern = lc_scan_kernel<M, MIXED>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return e;
