@@ -354,17 +354,17 @@ __device__ __noinline__ void block_sort_regs(u64* sk, int32_t* ss, int q) {
         k[e] = i < q ? sk[i] : KEY_MAX;
         v[e] = i < q ? ss[i] : 0;
     }
-    // one compare-exchange of registers e < e2 in the direction of merge size `size`
+    // one compare-exchange of registers e < e2 in the direction of merge size `size` (selects, no
+    // branches: the lanes of a warp disagree on the swap)
     auto cx = [&](int e, int e2, int size) {
         const bool asc = ((tid * PER + e) & size) == 0;
-        if ((k[e] > k[e2]) == asc) {
-            const u64 tk = k[e];
-            k[e] = k[e2];
-            k[e2] = tk;
-            const int32_t tv = v[e];
-            v[e] = v[e2];
-            v[e2] = tv;
-        }
+        const u64 a = k[e], b = k[e2];
+        const int32_t va = v[e], vb = v[e2];
+        const bool sw = (a > b) == asc;
+        k[e] = sw ? b : a;
+        k[e2] = sw ? a : b;
+        v[e] = sw ? vb : va;
+        v[e2] = sw ? va : vb;
     };
     // the stages of one merge with partners PER / 2, ..., 1 apart: within the thread
     auto local_stages = [&](int size) {
@@ -403,10 +403,8 @@ __device__ __noinline__ void block_sort_regs(u64* sk, int32_t* ss, int q) {
                     ov = __shfl_xor_sync(0xffffffffu, v[e], j / PER);
                 }
                 const bool take = (lower == asc) ? ok < k[e] : ok > k[e];
-                if (take) {
-                    k[e] = ok;
-                    v[e] = ov;
-                }
+                k[e] = take ? ok : k[e];
+                v[e] = take ? ov : v[e];
             }
         }
         local_stages(size);

@@ -718,7 +718,7 @@ __device__ __forceinline__ void refine_rerank(const DevIndex& ix, const ScanArgs
 // The sort carries the keys and, with them, either base ids (the exact form) or hand-off slots
 // (precision form, refinement re-rank: the slot leads to the candidate's code row and list).
 template <bool MIXED, int M, int NT>
-__global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 3) : 0) finalize_kernel(DevIndex ix, ScanArgs a) {
+__global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 4) : 0) finalize_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     constexpr int FIN_NT = NT;
     const int n2 = a.cand_stride;  // power of two
