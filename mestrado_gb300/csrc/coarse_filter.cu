@@ -47,7 +47,7 @@ static size_t cand_select_smem(int w, int cap, int d) {
     const int kcap = pow2_ge(std::max(w, 2));
     const int bcap = std::max(std::max(cap, 2 * CC_NT), kcap);
     return sizeof(u64) * (2 * (size_t)kcap + bcap + 1) + TOPK_WORK_BYTES + 2 * sizeof(int) + sizeof(float) * d +
-           sizeof(int) * CC_NT + sizeof(float) * CC_NT * (CC_KC + 1) + sizeof(int) * (CC_MAX_REGIONS + 4);
+           sizeof(int) * CC_NT + sizeof(float) * CC_NT * (CC_KC + 1) + sizeof(int) * (2 * CC_MAX_REGIONS + 5);
 }
 
 bool coarse_filter_shape(int C, int w, int d, int* S, int* r, int* cap) {
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
     float* rows = reinterpret_cast<float*>(ids + CC_NT);  // [CC_NT][CC_KC + 1]
     int* rcnt = reinterpret_cast<int*>(rows + CC_NT * (CC_KC + 1));  // [CC_MAX_REGIONS] survivor counts
     int* tally = rcnt + CC_MAX_REGIONS;                               // candidates, below, overflow
+    int* rpre = tally + 4;                                            // [CC_MAX_REGIONS + 1] prefix of rcnt
     TopKSmem s{best, tmp, buf, cnt, cnt + 1, thresh, 0, kcap, bcap, work};
     const int q = blockIdx.x, tid = threadIdx.x;
     for (int l = tid; l < d; l += CC_NT) xq[l] = X[(int64_t)q * d + l];
@@ -195,23 +196,61 @@ __global__ void __launch_bounds__(CC_NT) coarse_cand_select_kernel(const float* 
             rcnt[g] = c;
         }
         __syncthreads();
+        // exclusive prefix of the region counts (thread t sums regions 4t .. 4t + 3), so that the loop
+        // below visits the survivors only, not every slot of the regions (sized for the batch's
+        // largest nprobe)
+        {
+            constexpr int PER = CC_MAX_REGIONS / CC_NT;
+            static_assert(PER * CC_NT == CC_MAX_REGIONS, "regions per thread");
+            int v[PER], sum = 0;
+#pragma unroll
+            for (int j = 0; j < PER; j++) {
+                const int g = tid * PER + j;
+                v[j] = g < G ? rcnt[g] : 0;
+                sum += v[j];
+            }
+            const int lane = tid & 31, warp = tid >> 5;
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int x = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += x;
+            }
+            __shared__ int wsum[CC_NT / 32];
+            if (lane == 31) wsum[warp] = incl;
+            __syncthreads();
+            int base = incl - sum;
+            for (int w2 = 0; w2 < warp; w2++) base += wsum[w2];
+#pragma unroll
+            for (int j = 0; j < PER; j++) {
+                const int g = tid * PER + j;
+                if (g < G) rpre[g] = base;
+                base += v[j];
+            }
+            if (tid == CC_NT - 1) rpre[G] = base;
+            __syncthreads();
+        }
+        const int nsurv = rpre[G];
         const float qf = (float)qn, qlen = sqrtf(qf), T = f.thr[q];
         const int2* sq = f.surv + (int64_t)q * G * f.sreg;
         int mine = 0;
 #pragma unroll 4
-        for (int e = tid; e < G * f.sreg; e += CC_NT) {
-            const int g = e / f.sreg, sl = e - g * f.sreg;
-            if (sl < rcnt[g]) {
-                const int2 v = sq[e];
-                const int c = v.x;
-                const float cn = cnorm[c];
-                const float a = qf + cn - 2.0f * __int_as_float(v.y);
-                const float ee = mixed_eps(qf, qlen, cn, f.clen[c]);
-                mine += (a + ee <= T) ? 1 : 0;
-                if (a - ee <= T) {
-                    const int slot = atomicAdd(&tally[0], 1);
-                    if (slot < f.cap) f.cand[(int64_t)q * f.cap + slot] = c;
-                }
+        for (int i = tid; i < nsurv; i += CC_NT) {
+            int lo = 0, hi = G;  // the region of survivor i: rpre[lo] <= i < rpre[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (rpre[mid] <= i) lo = mid;
+                else hi = mid;
+            }
+            const int2 v = sq[(int64_t)lo * f.sreg + (i - rpre[lo])];
+            const int c = v.x;
+            const float cn = cnorm[c];
+            const float a = qf + cn - 2.0f * __int_as_float(v.y);
+            const float ee = mixed_eps(qf, qlen, cn, f.clen[c]);
+            mine += (a + ee <= T) ? 1 : 0;
+            if (a - ee <= T) {
+                const int slot = atomicAdd(&tally[0], 1);
+                if (slot < f.cap) f.cand[(int64_t)q * f.cap + slot] = c;
             }
         }
         if (mine) atomicAdd(&tally[1], mine);
