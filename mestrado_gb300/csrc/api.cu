@@ -134,6 +134,7 @@ struct gbivf_index {
     // hand-off lists of the precision form and the refinement re-rank; the precision form's count of
     // queries whose result its finalize could not prove equal to the exact form's
     DBuf w_clist, w_unproven;
+    DBuf w_rs;                        // the precision form's re-score workspace (RescoreWork)
     bool last_mixed = false;          // the last search used the precision form of the scan
     // list-centric scan (scan_lists.cu): one workspace block, its layout, stage events
     DBuf lc_ws;
@@ -174,7 +175,7 @@ void free_index(gbivf_index* ix) {
                     &ix->w_cdist, &ix->w_ids, &ix->w_dis, &ix->w_res, &ix->w_start, &ix->w_queue,
                     &ix->w_ckey, &ix->w_cid, &ix->w_ccnt, &ix->coa_tiles, &ix->coa_len, &ix->coa_colG, &ix->coa_colK, &ix->w_qtiles, &ix->w_flags,
                     &ix->w_thr, &ix->w_fcnt, &ix->w_cand, &ix->w_surv, &ix->w_scnt, &ix->w_clist,
-                    &ix->w_unproven, &ix->pq2, &ix->codes2, &ix->lc_ws})
+                    &ix->w_unproven, &ix->w_rs, &ix->pq2, &ix->codes2, &ix->lc_ws})
         b->release();
     if (ix->stream) cudaStreamDestroy(ix->stream);
     ix->stream = nullptr;
@@ -462,6 +463,25 @@ int run_scan(gbivf_index* ix, ScanArgs& a, cudaStream_t st, cudaEvent_t mid = nu
             CK(ix->w_unproven.ensure(sizeof(int)));
             CK(cudaMemsetAsync(ix->w_unproven.p, 0, sizeof(int), st));
             a.unproven = ix->w_unproven.as<int>();
+            // the re-score's workspace, one block: list, marks, counts, bounds, the two chunk queues
+            const size_t nq = (size_t)a.nq, sd = (size_t)stride;
+            const int qcap = rescore_queue_cap(a.nq, stride);
+            auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+            const size_t o_list = 0, o_marks = o_list + up(4 * nq * sd), o_cnt = o_marks + up(nq * sd / 8),
+                         o_t0 = o_cnt + up(8 * nq), o_amax = o_t0 + up(8 * nq), o_r2 = o_amax + up(8 * nq),
+                         o_queue = o_r2 + up(4 * nq), o_qcount = o_queue + up(2 * 16 * (size_t)qcap),
+                         total = o_qcount + 256;
+            CK(ix->w_rs.ensure(total));
+            unsigned char* b = static_cast<unsigned char*>(ix->w_rs.p);
+            a.rw.list = reinterpret_cast<int32_t*>(b + o_list);
+            a.rw.marks = reinterpret_cast<unsigned*>(b + o_marks);
+            a.rw.cnt = reinterpret_cast<int*>(b + o_cnt);
+            a.rw.t0 = reinterpret_cast<unsigned long long*>(b + o_t0);
+            a.rw.amax = reinterpret_cast<unsigned long long*>(b + o_amax);
+            a.rw.r2 = reinterpret_cast<float*>(b + o_r2);
+            a.rw.queue = reinterpret_cast<int4*>(b + o_queue);
+            a.rw.qcount = reinterpret_cast<int*>(b + o_qcount);
+            a.rw.qcap = qcap;
         }
         if (lists) {
             if (!(a.flags & (SCAN_MIXED | SCAN_REFINE))) {  // the select kernel writes lists only for those

@@ -41,6 +41,20 @@ struct DevIndex {
     const uint8_t* codes2 = nullptr;
 };
 
+// The precision form's exact re-score (scan_persistent.cu, launch_finalize): per-query selects and
+// gathers around a flat re-score kernel that works through queues of 32-candidate chunks.
+struct RescoreWork {
+    int32_t* list = nullptr;            // nq x cand_stride: hand-off slots to re-score, first round then second
+    int* cnt = nullptr;                 // nq x 2: list length after the first round, after the second
+    unsigned* marks = nullptr;          // nq x cand_stride / 32: slots of the first round
+    unsigned long long* t0 = nullptr;   // nq: largest exact key of the first round
+    unsigned long long* amax = nullptr; // nq: largest approximate key of the hand-off
+    float* r2 = nullptr;                // nq: largest squared residual norm over the query's probes
+    int4* queue = nullptr;              // 2 x qcap chunks (query, first, end, 0), one queue per round
+    int* qcount = nullptr;              // [0], [1]: chunks queued per round
+    int qcap = 0;
+};
+
 struct ScanArgs {
     int nq = 0, w = 0, k = 0, kl = 0, flags = 0;
     const float* queries = nullptr;    // nq x d
@@ -79,6 +93,8 @@ struct ScanArgs {
     // precision form: incremented by finalize for each query whose result it could not prove equal
     // to the exact form's (NULL: not counted)
     int* unproven = nullptr;
+    // precision form: the re-score's workspace (required with SCAN_MIXED)
+    RescoreWork rw;
 };
 
 // the precision form's approximate selection for a query returning kk results:
@@ -123,6 +139,8 @@ cudaError_t launch_finalize(const DevIndex& ix, const ScanArgs& a, cudaStream_t 
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
+// chunks per round of the precision form's re-score queue for nq queries and a hand-off stride
+int rescore_queue_cap(int nq, int stride);
 
 // List-centric scan (scan_lists.cu): the (query, list) pairs of a batch grouped by list, G queries
 // per work item. Device workspace, sized by the host for nq queries, C lists and at most

@@ -717,236 +717,16 @@ __device__ __forceinline__ void refine_rerank(const DevIndex& ix, const ScanArgs
 // Per query (one CTA): order the hand-off set, then write it, or re-rank it and write the k best.
 // The sort carries the keys and, with them, either base ids (the exact form) or hand-off slots
 // (precision form, refinement re-rank: the slot leads to the candidate's code row and list).
-template <bool MIXED, int M, int NT>
-__global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 4) : 0) finalize_kernel(DevIndex ix, ScanArgs a) {
-    extern __shared__ __align__(16) unsigned char fsm[];
+// The results of one query from its ordered set: keys[0 .. n) ascending with ids[0 .. n) (base ids,
+// or hand-off slots when `slots`), written out, or re-ranked first (RERANK by the raw vectors,
+// REFINE by the refinement codes). keys[] holds room for the next power of two >= n; xq is the
+// query (shared memory) when re-ranking. All NT threads of the block call it.
+template <int M, int NT>
+__device__ void fin_output(const DevIndex& ix, const ScanArgs& a, int q, int64_t hb, u64* keys, int32_t* ids, int n,
+                           const float* xq, bool slots) {
     constexpr int FIN_NT = NT;
-    const int n2 = a.cand_stride;  // power of two
-    u64* keys = reinterpret_cast<u64*>(fsm);
-    int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
-    float* xq = reinterpret_cast<float*>(ids + n2);
-    const int q = blockIdx.x, tid = threadIdx.x;
+    const int tid = threadIdx.x;
     const bool rerank = a.flags & SCAN_RERANK, refine = a.flags & SCAN_REFINE;
-    const bool slots = MIXED || refine;  // ids[] holds hand-off slots, not base ids
-    const int64_t hb = (int64_t)q * n2;  // this query's hand-off slots
-    int n = a.cand_cnt[q];
-    // only this query's candidates are sorted: the smallest power of two holding them (the
-    // hand-off pads with KEY_MAX), not the batch-wide stride
-    int p2 = 2;
-    while (p2 < n) p2 <<= 1;
-    for (int c = tid; c < p2; c += FIN_NT) {
-        keys[c] = c < n ? a.cand_key[hb + c] : KEY_MAX;
-        ids[c] = slots ? c : a.cand_id[hb + c];
-    }
-    if (rerank || slots)
-        for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
-    __syncthreads();
-    if constexpr (MIXED) {
-        // Exact re-score of the approximate candidates that can still belong to the exact top-kk,
-        // keyed (distance, position) as the plain form keys them. Every approximate distance A
-        // bounds the exact one E from below: E >= A (1 - MIX_DELTA) - eps_q, where MIX_DELTA covers
-        // the FP16 rounding of the table entries (2^-11 relative, summed in FP32) and eps_q the FP32
-        // rounding of both forms' expansions (at most ~2^-16 (||r||^2 + sum_s max ||c_s||^2)), with
-        // a margin of 4 and 16. So, with T0 the largest exact distance of the kk best approximate
-        // candidates, no candidate with A >= tau = (T0 + eps_q) / (1 - MIX_DELTA) can enter the
-        // exact top-kk: those below tau are re-scored, the rest are not.
-        // Neither set is sorted: the kk-th approximate key is found by a radix select, the
-        // candidates to re-score are gathered into a list (ids[], whose identity contents this form
-        // does not need), and only the final kk exact keys are sorted, in registers.
-        static_assert(NT == FIN_NT && NT * FIN_SORT_PER >= 1024, "the final sort holds kl <= 1024 keys");
-        // the final sort's staging (d = 128): keys, then slots, each for NT * FIN_SORT_PER + FIN_XTRA
-        u64* sk = reinterpret_cast<u64*>(xq + 128);
-        int32_t* ss = reinterpret_cast<int32_t*>(sk + NT * FIN_SORT_PER + FIN_XTRA);
-        int32_t* list = ids;
-        const int kk0 = (rerank || refine) ? a.kl : query_k(a, q);
-        const int ksel = mixed_sel(a, kk0);
-        const int kk = min(n, kk0);
-        const int lane = tid & 31;
-        __shared__ unsigned s_flag[4096 / 32];  // bit c: candidate c re-scored (n <= sel_cap <= 4096)
-        __shared__ u64 s_t0, s_amax;
-        __shared__ unsigned s_r2;
-        __shared__ int s_cnt, s_cnt2;
-        for (int i = tid; i < 4096 / 32; i += NT) s_flag[i] = 0u;
-        if (tid == 0) {
-            s_t0 = 0;
-            s_amax = 0;
-            s_r2 = 0u;
-            s_cnt = 0;
-            s_cnt2 = 0;
-        }
-        u64 amax = 0;
-        for (int c = tid; c < n; c += NT) amax = keys[c] > amax ? keys[c] : amax;
-        __syncthreads();
-        atomicMax(&s_amax, amax);
-        const u64 th = n > kk ? block_kth_flagged(keys, n, nullptr, kk) : KEY_MAX;
-        // gather the candidates passing `pred` into list[s_cnt ..) and mark them (warp-uniform
-        // loop: each 32-candidate word of the marks belongs to one warp)
-        auto gather = [&](auto pred) {
-            for (int c0 = tid & ~31; c0 < n; c0 += NT) {
-                const int c = c0 + lane;
-                const bool in = c < n && pred(c);
-                const unsigned mk = __ballot_sync(0xffffffffu, in);
-                if (mk == 0u) continue;
-                int base = 0;
-                if (lane == 0) {
-                    base = atomicAdd(&s_cnt, __popc(mk));
-                    s_flag[c0 >> 5] |= mk;
-                }
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (in) list[base + __popc(mk & ((1u << lane) - 1u))] = c;
-            }
-        };
-        gather([&](int c) { return keys[c] <= th; });
-        __syncthreads();
-        const int m0 = s_cnt;
-        int m = m0;
-        // two rounds of exact re-scores (one copy of the loop): list[0 .. m0), then list[m0 .. m).
-        // Before each, one pass fetches the candidates' lists and code rows into meta[] (the final
-        // sort's staging, free until then) and asks L2 for their code rows and list centroids, so
-        // the re-score loop starts from on-chip data instead of three dependent memory round trips.
-        int2* meta = reinterpret_cast<int2*>(sk);  // NT * FIN_SORT_PER entries: (list, row)
-        constexpr int META = NT * FIN_SORT_PER;
-        u64 t0 = 0;
-        for (int round = 0, i0 = 0; round < 2; round++) {
-            for (int i = i0 + tid; i < min(m, META); i += NT) {
-                const int c = list[i];
-                const int l = a.cand_list[hb + c], row = a.cand_id[hb + c];
-                meta[i] = make_int2(l, row);
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(ix.codes + (int64_t)row * M)));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(ix.coa + (int64_t)l * 128)));
-            }
-            __syncthreads();
-            for (int i = i0 + tid; i < m; i += NT) {
-                const int c = list[i];
-                const int2 lr = i < META ? meta[i] : make_int2(a.cand_list[hb + c], a.cand_id[hb + c]);
-                const u64 key = make_key(exact_adc<M>(ix, xq, lr.x, lr.y), key_payload(keys[c]));
-                keys[c] = key;
-                t0 = key > t0 ? key : t0;
-            }
-            if (round == 1) break;
-            // the largest squared residual norm over the query's probes (a bound on ||r||^2 for
-            // every candidate, handed off or not): four threads per probe, 32 dimensions each
-            float r2 = 0.0f;
-            const int wq = query_w(a, q);
-            for (int j0 = 0; j0 < wq; j0 += NT / 4) {  // block-uniform trip count (shuffles below)
-                const int j = j0 + tid / 4, part = tid & 3;
-                float sq = 0.0f;
-                const int l = j < wq ? a.probes[(int64_t)q * a.w + j] : -1;
-                if (l >= 0 && l < ix.C) {
-                    const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128 + 32 * part);
-                    const float* xp = xq + 32 * part;
-                    float4 y[8];
-#pragma unroll
-                    for (int v = 0; v < 8; v++) y[v] = __ldg(y4 + v);
-#pragma unroll
-                    for (int v = 0; v < 8; v++) {
-                        const float d0 = xp[4 * v] - y[v].x, d1 = xp[4 * v + 1] - y[v].y, d2 = xp[4 * v + 2] - y[v].z,
-                                    d3 = xp[4 * v + 3] - y[v].w;
-                        sq = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, sq))));
-                    }
-                }
-                sq += __shfl_xor_sync(0xffffffffu, sq, 1);
-                sq += __shfl_xor_sync(0xffffffffu, sq, 2);
-                r2 = fmaxf(r2, sq);
-            }
-            atomicMax(&s_t0, t0);
-            atomicMax(&s_r2, __float_as_uint(r2));  // (non-negative floats order as their bits)
-            __syncthreads();
-            const double T0 = fmax(0.0, (double)key_dist(s_t0));
-            const double eps = MIX_EPS_REL * ((double)__uint_as_float(s_r2) * (1.0 + 0x1p-10) + (double)ix.pq_cmax) +
-                               MIX_EPS_ABS;
-            const double tau = (T0 + eps) / (1.0 - MIX_DELTA) * (1.0 + 0x1p-20);
-            // the rest of the candidates below tau (their keys are still approximate)
-            gather([&](int c) { return !((s_flag[c >> 5] >> (c & 31)) & 1u) && (double)key_dist(keys[c]) < tau; });
-            // not proven: the hand-off is full (candidates may lie beyond it) and all of it is below tau
-            if (tid == 0 && a.unproven && n >= ksel && (double)key_dist(s_amax) < tau) atomicAdd(a.unproven, 1);
-            __syncthreads();
-            i0 = m0;
-            m = s_cnt;
-        }
-        __syncthreads();
-        // The kk best exact keys of the re-scored set, in order. The first round's set holds
-        // min(n, kk) keys and the second round usually adds a few: both are sorted (the first in
-        // registers, the second by rank) and merged, each key's place being its rank in its own set
-        // plus the number of smaller keys in the other. A large second set goes through a radix
-        // select of the kk-th key and one sort instead.
-        u64* xk = sk + META;                                   // second set: FIN_XTRA keys ...
-        int32_t* xs = reinterpret_cast<int32_t*>(ss + META);   // ... and slots
-        const int m1 = m - m0;
-        if (m1 <= FIN_XTRA) {
-            for (int i = tid; i < m0; i += NT) {
-                sk[i] = keys[list[i]];
-                ss[i] = list[i];
-            }
-            for (int i = tid; i < m1; i += NT) {
-                xk[i] = keys[list[m0 + i]];
-                xs[i] = list[m0 + i];
-            }
-            __syncthreads();
-            if (m0 <= RANK_SORT_MAX) rank_sort(sk, ss, m0);
-            else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, m0);
-            if (m1 > 1) rank_sort(xk, xs, m1);
-            // (both sorts end with a barrier)
-            const int nout = min(m, kk0);
-            for (int i = tid; i < m0; i += NT) {
-                const u64 key = sk[i];
-                int lo = 0, hi = m1;  // smaller keys of the second set
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (xk[mid] < key) lo = mid + 1;
-                    else hi = mid;
-                }
-                if (i + lo < nout) {
-                    keys[i + lo] = key;
-                    ids[i + lo] = ss[i];
-                }
-            }
-            for (int i = tid; i < m1; i += NT) {
-                const u64 key = xk[i];
-                int lo = 0, hi = m0;  // smaller keys of the first set
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (sk[mid] < key) lo = mid + 1;
-                    else hi = mid;
-                }
-                if (i + lo < nout) {
-                    keys[i + lo] = key;
-                    ids[i + lo] = xs[i];
-                }
-            }
-            __syncthreads();
-            n = nout;
-        } else {
-            const u64 th2 = m > kk ? block_kth_flagged(keys, n, s_flag, kk) : KEY_MAX;
-            for (int c0 = tid & ~31; c0 < n; c0 += NT) {
-                const int c = c0 + lane;
-                const bool in = c < n && ((s_flag[c >> 5] >> (c & 31)) & 1u) && keys[c] <= th2;
-                const unsigned mk = __ballot_sync(0xffffffffu, in);
-                if (mk == 0u) continue;
-                int base = 0;
-                if (lane == 0) base = atomicAdd(&s_cnt2, __popc(mk));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (in) {
-                    const int o = base + __popc(mk & ((1u << lane) - 1u));
-                    sk[o] = keys[c];
-                    ss[o] = c;
-                }
-            }
-            __syncthreads();
-            const int nout = s_cnt2;  // min(m, kk): the keys are unique
-            if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
-            else block_sort_regs<NT, FIN_SORT_PER>(sk, ss, nout);
-            for (int c = tid; c < nout; c += NT) {
-                keys[c] = sk[c];
-                ids[c] = ss[c];
-            }
-            __syncthreads();
-            n = nout;
-        }
-    } else {
-        if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);
-        else bitonic_sort_pairs(keys, ids, p2);
-    }
     auto base_id = [&](int c) { return slots ? ix.ids[a.cand_id[hb + ids[c]]] : ids[c]; };
     const float inf = __int_as_float(0x7f800000);
     if (!rerank && !refine) {
@@ -1010,6 +790,38 @@ __global__ void __launch_bounds__(NT, MIXED ? (M == 4 ? 2 : 4) : 0) finalize_ker
     }
 }
 
+// Per query (one CTA): sort the hand-off set, then write it, or re-rank it by
+// exact L2 (ivf_search.cpp:113-134) and write the k best. (The precision form's hand-off goes
+// through the re-score kernels below instead.)
+template <int M, int NT>
+__global__ void __launch_bounds__(NT) finalize_kernel(DevIndex ix, ScanArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    constexpr int FIN_NT = NT;
+    const int n2 = a.cand_stride;  // power of two
+    u64* keys = reinterpret_cast<u64*>(fsm);
+    int32_t* ids = reinterpret_cast<int32_t*>(keys + n2);
+    float* xq = reinterpret_cast<float*>(ids + n2);
+    const int q = blockIdx.x, tid = threadIdx.x;
+    const bool rerank = a.flags & SCAN_RERANK, refine = a.flags & SCAN_REFINE;
+    const bool slots = refine;  // ids[] holds hand-off slots, not base ids
+    const int64_t hb = (int64_t)q * n2;  // this query's hand-off slots
+    const int n = a.cand_cnt[q];
+    // only this query's candidates are sorted: the smallest power of two holding them (the
+    // hand-off pads with KEY_MAX), not the batch-wide stride
+    int p2 = 2;
+    while (p2 < n) p2 <<= 1;
+    for (int c = tid; c < p2; c += FIN_NT) {
+        keys[c] = c < n ? a.cand_key[hb + c] : KEY_MAX;
+        ids[c] = slots ? c : a.cand_id[hb + c];
+    }
+    if (rerank || slots)
+        for (int x = tid; x < ix.d; x += FIN_NT) xq[x] = a.queries[(int64_t)q * ix.d + x];
+    __syncthreads();
+    if (n <= RANK_SORT_MAX) rank_sort(keys, ids, n);
+    else bitonic_sort_pairs(keys, ids, p2);
+    fin_output<M, NT>(ix, a, q, hb, keys, ids, n, xq, slots);
+}
+
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a) {
     const int kk = (a.flags & (SCAN_RERANK | SCAN_REFINE)) ? a.kl : a.k;
     const bool m_ok = ix.m == 4 || ix.m == 8 || ix.m == 16;
@@ -1028,21 +840,345 @@ int scan_persistent_stride(const ScanArgs& a) {
     return pow2_at_least(std::max(std::max(sel, a.k), 2));
 }
 
+// ---------------------------------------------------------------------------
+// The precision form's exact re-score.
+//
+// Every approximate distance A bounds the exact one E (the reference's FP32 arithmetic) from
+// below: E >= A (1 - MIX_DELTA) - eps_q. MIX_DELTA covers the FP16 rounding of the table entries
+// (2^-11 relative, a saturated entry only lowers A) and the FP32 accumulation; eps_q the FP32
+// rounding of both forms' expansions (at most ~2^-16 (||r||^2 + sum_s max ||c_s||^2)), with
+// margins of 4 and 16. So, with T0 the largest exact distance of the kk best approximate
+// candidates, no candidate with A >= tau = (T0 + eps_q) / (1 - MIX_DELTA) can enter the exact
+// top-kk: the kk best and those below tau are re-scored, no other. Five launches:
+//   rs_first_kernel   per query: the kk-th approximate key (radix select), the kk best listed
+//                     (round 1), the residual bound r2;
+//   rs_rescore_kernel flat: one lane per listed candidate, 32-candidate chunks from a queue; the
+//                     exact key replaces the approximate one in the hand-off; T0 by atomicMax;
+//   rs_second_kernel  per query: tau, the other candidates below it listed (round 2), the proof;
+//   rs_rescore_kernel round 2;
+//   rs_order_kernel   per query: the two rounds sorted (registers / by rank) and merged, then the
+//                     results written (or re-ranked) by fin_output.
+// Only the re-score kernel holds the exact arithmetic's registers; the per-query kernels run at
+// the occupancy their shared memory allows.
+// ---------------------------------------------------------------------------
+
+constexpr int RS_NT = 128;        // per-query kernels
+constexpr int RS_CHUNK = 32;      // candidates per queue entry (one warp)
+
+// queue the chunks [i0, i1) of query q's list in round `round`
+__device__ __forceinline__ void rs_enqueue(const ScanArgs& a, int round, int q, int i0, int i1) {
+    const int nch = (i1 - i0 + RS_CHUNK - 1) / RS_CHUNK;
+    __shared__ int s_base;
+    if (threadIdx.x == 0) s_base = nch > 0 ? atomicAdd(a.rw.qcount + round, nch) : 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < nch; j += blockDim.x) {
+        const int slot = s_base + j;
+        if (slot < a.rw.qcap) a.rw.queue[(int64_t)round * a.rw.qcap + slot] = make_int4(q, i0 + j * RS_CHUNK, i1, 0);
+    }
+}
+
+// warp-uniform gather of the candidates c < n passing pred(c) into list[*cnt ..); returns the
+// warp's ballot word for the 32 candidates from c0
+template <class Pred>
+__device__ __forceinline__ unsigned rs_gather_word(int c0, int n, int32_t* list, int* cnt, Pred pred) {
+    const int lane = threadIdx.x & 31, c = c0 + lane;
+    const bool in = c < n && pred(c);
+    const unsigned mk = __ballot_sync(0xffffffffu, in);
+    int base = 0;
+    if (lane == 0 && mk) base = atomicAdd(cnt, __popc(mk));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (in) list[base + __popc(mk & ((1u << lane) - 1u))] = c;
+    return mk;
+}
+
+template <int M>
+__global__ void __launch_bounds__(RS_NT) rs_first_kernel(DevIndex ix, ScanArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    u64* keys = reinterpret_cast<u64*>(fsm);   // [cand_stride] the approximate keys
+    float* xq = reinterpret_cast<float*>(keys + a.cand_stride);
+    __shared__ u64 s_amax;
+    __shared__ unsigned s_r2;
+    __shared__ int s_cnt;
+    const int q = blockIdx.x, tid = threadIdx.x, stride = a.cand_stride;
+    const int64_t hb = (int64_t)q * stride;
+    const int n = a.cand_cnt[q];
+    const bool rr = a.flags & (SCAN_RERANK | SCAN_REFINE);
+    const int kk = min(n, rr ? a.kl : query_k(a, q));
+    if (tid == 0) {
+        s_amax = 0;
+        s_r2 = 0u;
+        s_cnt = 0;
+    }
+    u64 amax = 0;
+    for (int c = tid; c < n; c += RS_NT) {
+        keys[c] = a.cand_key[hb + c];
+        amax = keys[c] > amax ? keys[c] : amax;
+    }
+    for (int x = tid; x < 128; x += RS_NT) xq[x] = a.queries[(int64_t)q * 128 + x];
+    __syncthreads();
+    atomicMax(&s_amax, amax);
+    const u64 th = n > kk ? block_kth_flagged(keys, n, nullptr, kk) : KEY_MAX;
+    int32_t* list = a.rw.list + hb;
+    unsigned* marks = a.rw.marks + (int64_t)q * (stride / 32);
+    for (int c0 = tid & ~31; c0 < n; c0 += RS_NT) {
+        const unsigned mk = rs_gather_word(c0, n, list, &s_cnt, [&](int c) { return keys[c] <= th; });
+        if ((tid & 31) == 0) marks[c0 >> 5] = mk;
+    }
+    // the largest squared residual norm over the query's probes (a bound on ||r||^2 for every
+    // candidate, handed off or not): four threads per probe, 32 dimensions each
+    float r2 = 0.0f;
+    const int wq = query_w(a, q);
+    for (int j0 = 0; j0 < wq; j0 += RS_NT / 4) {  // block-uniform trip count (shuffles below)
+        const int j = j0 + tid / 4, part = tid & 3;
+        float sq = 0.0f;
+        const int l = j < wq ? a.probes[(int64_t)q * a.w + j] : -1;
+        if (l >= 0 && l < ix.C) {
+            const float4* y4 = reinterpret_cast<const float4*>(ix.coa + (int64_t)l * 128 + 32 * part);
+            const float* xp = xq + 32 * part;
+            float4 y[8];
+#pragma unroll
+            for (int v = 0; v < 8; v++) y[v] = __ldg(y4 + v);
+#pragma unroll
+            for (int v = 0; v < 8; v++) {
+                const float d0 = xp[4 * v] - y[v].x, d1 = xp[4 * v + 1] - y[v].y, d2 = xp[4 * v + 2] - y[v].z,
+                            d3 = xp[4 * v + 3] - y[v].w;
+                sq = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, fmaf(d3, d3, sq))));
+            }
+        }
+        sq += __shfl_xor_sync(0xffffffffu, sq, 1);
+        sq += __shfl_xor_sync(0xffffffffu, sq, 2);
+        r2 = fmaxf(r2, sq);
+    }
+    atomicMax(&s_r2, __float_as_uint(r2));  // (non-negative floats order as their bits)
+    __syncthreads();
+    const int m0 = s_cnt;
+    if (tid == 0) {
+        a.rw.cnt[2 * q] = m0;
+        a.rw.cnt[2 * q + 1] = m0;
+        a.rw.t0[q] = 0;
+        a.rw.amax[q] = s_amax;
+        a.rw.r2[q] = __uint_as_float(s_r2);
+    }
+    rs_enqueue(a, 0, q, 0, m0);
+}
+
+// one lane per listed candidate: its exact ADC distance (exact_adc: the reference's arithmetic, the
+// exact form's table entries bit for bit) keyed (distance, position) in place of its approximate key
+template <int M>
+__global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 4) rs_rescore_kernel(DevIndex ix, ScanArgs a, int round) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (RS_NT / 32);
+    const int nch = min(a.rw.qcount[round], a.rw.qcap);
+    const int4* queue = a.rw.queue + (int64_t)round * a.rw.qcap;
+    for (int ch = blockIdx.x * (RS_NT / 32) + (threadIdx.x >> 5); ch < nch; ch += nwarps) {
+        const int4 e = queue[ch];  // (query, first, end, 0)
+        const int q = e.x, i = e.y + lane;
+        const int64_t hb = (int64_t)q * a.cand_stride;
+        u64 key = 0;
+        if (i < e.z) {
+            const int c = a.rw.list[hb + i];
+            key = make_key(exact_adc<M>(ix, a.queries + (int64_t)q * 128, a.cand_list[hb + c], a.cand_id[hb + c]),
+                           key_payload(a.cand_key[hb + c]));
+            a.cand_key[hb + c] = key;
+        }
+        if (round == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const u64 x = __shfl_xor_sync(0xffffffffu, key, o);
+                key = x > key ? x : key;
+            }
+            if (lane == 0) atomicMax(a.rw.t0 + q, key);
+        }
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(RS_NT) rs_second_kernel(DevIndex ix, ScanArgs a) {
+    __shared__ int s_cnt;
+    const int q = blockIdx.x, tid = threadIdx.x, stride = a.cand_stride;
+    const int64_t hb = (int64_t)q * stride;
+    const int n = a.cand_cnt[q];
+    const bool rr = a.flags & (SCAN_RERANK | SCAN_REFINE);
+    const int ksel = mixed_sel(a, rr ? a.kl : query_k(a, q));
+    const int m0 = a.rw.cnt[2 * q];
+    const double T0 = fmax(0.0, (double)key_dist(a.rw.t0[q]));
+    const double eps = MIX_EPS_REL * ((double)a.rw.r2[q] * (1.0 + 0x1p-10) + (double)ix.pq_cmax) + MIX_EPS_ABS;
+    const double tau = (T0 + eps) / (1.0 - MIX_DELTA) * (1.0 + 0x1p-20);
+    if (tid == 0) s_cnt = m0;
+    __syncthreads();
+    int32_t* list = a.rw.list + hb;
+    const unsigned* marks = a.rw.marks + (int64_t)q * (stride / 32);
+    for (int c0 = tid & ~31; c0 < n; c0 += RS_NT) {
+        const unsigned mw = marks[c0 >> 5];
+        rs_gather_word(c0, n, list, &s_cnt, [&](int c) {
+            return !((mw >> (c & 31)) & 1u) && (double)key_dist(a.cand_key[hb + c]) < tau;
+        });
+    }
+    __syncthreads();
+    const int m = s_cnt;
+    if (tid == 0) {
+        a.rw.cnt[2 * q + 1] = m;
+        // not proven: the hand-off is full (candidates may lie beyond it) and all of it is below tau
+        if (a.unproven && n >= ksel && (double)key_dist(a.rw.amax[q]) < tau) atomicAdd(a.unproven, 1);
+    }
+    rs_enqueue(a, 1, q, m0, m);
+}
+
+// The kk best exact keys of the re-scored set, in order: the first round's set (min(n, kk) keys)
+// sorted in registers, the second (usually a few) by rank, the two merged -- each key's place is
+// its rank in its own set plus the number of smaller keys in the other; a large second set goes
+// through a radix select of the kk-th key and one sort instead. Then the results.
+template <int M>
+__global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    constexpr int META = RS_NT * FIN_SORT_PER;
+    const int stride = a.cand_stride;
+    u64* keys = reinterpret_cast<u64*>(fsm);                       // [stride] ordered keys, then scratch
+    int32_t* ids = reinterpret_cast<int32_t*>(keys + stride);      // [stride] their hand-off slots
+    float* xq = reinterpret_cast<float*>(ids + stride);            // [128] the query
+    u64* sk = reinterpret_cast<u64*>(xq + 128);                    // staging: META + FIN_XTRA keys ...
+    int32_t* ss = reinterpret_cast<int32_t*>(sk + META + FIN_XTRA);  // ... and slots
+    u64* xk = sk + META;
+    int32_t* xs = ss + META;
+    __shared__ int s_cnt2;
+    const int q = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    const int64_t hb = (int64_t)q * stride;
+    const bool rr = a.flags & (SCAN_RERANK | SCAN_REFINE);
+    const int kk0 = rr ? a.kl : query_k(a, q);
+    const int m0 = a.rw.cnt[2 * q], m = a.rw.cnt[2 * q + 1], m1 = m - m0;
+    const int32_t* list = a.rw.list + hb;
+    if (rr)
+        for (int x = tid; x < 128; x += RS_NT) xq[x] = a.queries[(int64_t)q * 128 + x];
+    if (tid == 0) s_cnt2 = 0;
+    int nout;
+    if (m1 <= FIN_XTRA) {
+        for (int i = tid; i < m0; i += RS_NT) {
+            const int c = list[i];
+            sk[i] = a.cand_key[hb + c];
+            ss[i] = c;
+        }
+        for (int i = tid; i < m1; i += RS_NT) {
+            const int c = list[m0 + i];
+            xk[i] = a.cand_key[hb + c];
+            xs[i] = c;
+        }
+        __syncthreads();
+        if (m0 <= RANK_SORT_MAX) rank_sort(sk, ss, m0);
+        else block_sort_regs<RS_NT, FIN_SORT_PER>(sk, ss, m0);
+        if (m1 > 1) rank_sort(xk, xs, m1);
+        __syncthreads();
+        nout = min(m, kk0);
+        for (int i = tid; i < m0; i += RS_NT) {
+            const u64 key = sk[i];
+            int lo = 0, hi = m1;  // smaller keys of the second set
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (xk[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+            if (i + lo < nout) {
+                keys[i + lo] = key;
+                ids[i + lo] = ss[i];
+            }
+        }
+        for (int i = tid; i < m1; i += RS_NT) {
+            const u64 key = xk[i];
+            int lo = 0, hi = m0;  // smaller keys of the first set
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (sk[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+            if (i + lo < nout) {
+                keys[i + lo] = key;
+                ids[i + lo] = xs[i];
+            }
+        }
+    } else {
+        // all m exact keys (m <= n <= stride) in keys[] / ids[], the kk0-th by a radix select
+        for (int i = tid; i < m; i += RS_NT) {
+            const int c = list[i];
+            keys[i] = a.cand_key[hb + c];
+            ids[i] = c;
+        }
+        __syncthreads();
+        const u64 th2 = m > kk0 ? block_kth_flagged(keys, m, nullptr, kk0) : KEY_MAX;
+        for (int c0 = tid & ~31; c0 < m; c0 += RS_NT) {
+            const int c = c0 + lane;
+            const bool in = c < m && keys[c] <= th2;
+            const unsigned mk = __ballot_sync(0xffffffffu, in);
+            int base = 0;
+            if (lane == 0 && mk) base = atomicAdd(&s_cnt2, __popc(mk));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (in) {
+                const int o = base + __popc(mk & ((1u << lane) - 1u));
+                sk[o] = keys[c];
+                ss[o] = ids[c];
+            }
+        }
+        __syncthreads();
+        nout = s_cnt2;  // min(m, kk0): the keys are unique
+        if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
+        else block_sort_regs<RS_NT, FIN_SORT_PER>(sk, ss, nout);
+        for (int c = tid; c < nout; c += RS_NT) {
+            keys[c] = sk[c];
+            ids[c] = ss[c];
+        }
+    }
+    __syncthreads();
+    fin_output<M, RS_NT>(ix, a, q, hb, keys, ids, nout, xq, true);
+}
+
+template <int M>
+static cudaError_t launch_rescore(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
+    const RescoreWork& w = a.rw;
+    if (!w.list || !w.cnt || !w.marks || !w.t0 || !w.amax || !w.r2 || !w.queue || !w.qcount || w.qcap <= 0 ||
+        ix.d != 128 || a.cand_stride > 4096 || a.cand_stride < 32)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(w.qcount, 0, 2 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const size_t sm1 = (size_t)a.cand_stride * 8 + 512;
+    if (sm1 > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(rs_first_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1)) != cudaSuccess)
+        return e;
+    rs_first_kernel<M><<<a.nq, RS_NT, sm1, st>>>(ix, a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int rgrid = sms * 4;  // persistent: the queues' lengths are known on the device only
+    rs_rescore_kernel<M><<<rgrid, RS_NT, 0, st>>>(ix, a, 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    rs_second_kernel<M><<<a.nq, RS_NT, 0, st>>>(ix, a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    rs_rescore_kernel<M><<<rgrid, RS_NT, 0, st>>>(ix, a, 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const size_t sm4 = (size_t)a.cand_stride * 12 + 512 + (size_t)(RS_NT * FIN_SORT_PER + FIN_XTRA) * 12;
+    if (sm4 > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(rs_order_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4)) != cudaSuccess)
+        return e;
+    rs_order_kernel<M><<<a.nq, RS_NT, sm4, st>>>(ix, a);
+    return cudaGetLastError();
+}
+
+// the re-score workspace's queue capacity for a batch (chunks of both rounds, per round)
+int rescore_queue_cap(int nq, int stride) { return nq * (stride / RS_CHUNK + 1); }
+
 template <int M, bool MIXED>
 static cudaError_t launch_fin(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
-    // keys, ids, the query; the precision form's final sort staging
-    const size_t fsm =
-        (size_t)a.cand_stride * 12 + 512 + (MIXED ? (size_t)(FIN_NT * FIN_SORT_PER + FIN_XTRA) * 12 : 0);
-    const bool big = !MIXED && (a.flags & SCAN_REFINE);
-    void (*fin)(DevIndex, ScanArgs) = finalize_kernel<MIXED, M, FIN_NT>;
-    if constexpr (!MIXED)
-        if (big) fin = finalize_kernel<false, M, FIN_NT_BIG>;
-    if (fsm > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
-        if (e != cudaSuccess) return e;
+    if constexpr (MIXED) {
+        return launch_rescore<M>(ix, a, st);
+    } else {
+        const size_t fsm = (size_t)a.cand_stride * 12 + 512;  // keys, ids, the query
+        const bool big = a.flags & SCAN_REFINE;
+        void (*fin)(DevIndex, ScanArgs) = big ? finalize_kernel<M, FIN_NT_BIG> : finalize_kernel<M, FIN_NT>;
+        if (fsm > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+            if (e != cudaSuccess) return e;
+        }
+        fin<<<a.nq, big ? FIN_NT_BIG : FIN_NT, fsm, st>>>(ix, a);
+        return cudaGetLastError();
     }
-    fin<<<a.nq, big ? FIN_NT_BIG : FIN_NT, fsm, st>>>(ix, a);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_finalize(const DevIndex& ix, const ScanArgs& a, cudaStream_t st) {
