@@ -375,7 +375,7 @@ int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
         return r;
     };
     const size_t o_w0 = take(4 * nq), o_pcnt = take(4 * C), o_pbeg = take(4 * (C + 1)), o_fill = take(4 * C),
-                 o_gbeg = take(4 * (C + 1)), o_pairs = take(16 * P), o_groups = take(16 * 9 * P), o_cnt = take(4 * 8),
+                 o_gbeg = take(4 * (C + 1)), o_bsum = take(8 * ((C + 4095) / 4096)), o_pairs = take(16 * P), o_groups = take(16 * 9 * P), o_cnt = take(4 * 8),
                  o_keys = take(8 * nq * a.cand_stride), o_cntA = take(4 * nq), o_tau = take(8 * nq),
                  o_tau0 = take(8 * nq), o_hist = take(4 * nq * (int64_t)LC_HIST_BUCKETS),
                  o_ebuf = take(8 * nq * (int64_t)w.ecap), o_ecnt = take(4 * nq), o_ovf = take(4 * nq);
@@ -386,6 +386,7 @@ int prepare_list_scan(gbivf_index* ix, const ScanArgs& a) {
     w.pbeg = reinterpret_cast<int*>(b + o_pbeg);
     w.fill = reinterpret_cast<int*>(b + o_fill);
     w.gbeg = reinterpret_cast<int*>(b + o_gbeg);
+    w.bsum = reinterpret_cast<int*>(b + o_bsum);
     w.pairs = reinterpret_cast<int4*>(b + o_pairs);
     w.groups = reinterpret_cast<int4*>(b + o_groups);
     w.counters = reinterpret_cast<int*>(b + o_cnt);  // [0..2] groups, work counter, overflows; [3], [4] queues

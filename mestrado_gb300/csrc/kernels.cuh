@@ -151,6 +151,7 @@ struct ListScanWork {
     int* pbeg = nullptr;      // C + 1: first pair of each list
     int* fill = nullptr;      // C: fill cursors
     int* gbeg = nullptr;      // C + 1: first group of each list
+    int* bsum = nullptr;      // 2 x ceil(C / 4096): per block of lists, its pairs and groups (the prefix sums)
     int4* pairs = nullptr;    // max_pairs: (query, probe, position of the probe's first row, 0), by list
     int4* groups = nullptr;   // max_pairs x (1 + G): work-item descriptors (scan_lists.cu)
     int* counters = nullptr;  // [0] groups, [1] work counter, [2] overflowed queries

@@ -98,78 +98,109 @@ __global__ void lc_plan_kernel(DevIndex ix, ScanArgs a, ListScanWork w, int beta
     }
 }
 
-// One block: exclusive prefix sums over the C lists of the pair counts (pbeg) and of the groups
-// of G pairs (gbeg); fill cursors start at pbeg; the totals go to pbeg[C], gbeg[C], counters[0].
-// The lists go by in chunks of 4 per thread (4,096 per pass): coalesced loads, a warp-shuffle scan,
-// the warps' totals scanned by warp 0, a running carry.
+// Prefix sums over the C lists of their pair counts (pbeg) and of their work items of G pairs
+// (gbeg); fill cursors start at pbeg; the totals go to pbeg[C], gbeg[C], counters[0]. Two launches
+// over blocks of LC_PFX lists (4 per thread): the blocks' totals, then each block's own scan from the
+// sum of the totals before it -- every block at once, instead of one block walking all C lists.
+constexpr int LC_PFX = 4096;
+
+template <int G>
+__device__ __forceinline__ void lc_prefix_load(int C, const ListScanWork& w, int i0, int (&c)[4], int& tp, int& tg) {
+    tp = tg = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        c[j] = i0 + j < C ? w.pcnt[i0 + j] : 0;
+        tp += c[j];
+        tg += (c[j] + G - 1) / G;
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(1024) lc_prefix_sums_kernel(int C, ListScanWork w) {
+    __shared__ int s_p[32], s_g[32];
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    int c[4], tp, tg;
+    lc_prefix_load<G>(C, w, blockIdx.x * LC_PFX + 4 * tid, c, tp, tg);
+    tp = __reduce_add_sync(0xffffffffu, tp);
+    tg = __reduce_add_sync(0xffffffffu, tg);
+    if (lane == 0) {
+        s_p[wp] = tp;
+        s_g[wp] = tg;
+    }
+    __syncthreads();
+    if (wp == 0) {
+        const int vp = __reduce_add_sync(0xffffffffu, s_p[lane]), vg = __reduce_add_sync(0xffffffffu, s_g[lane]);
+        if (lane == 0) {
+            w.bsum[2 * blockIdx.x] = vp;
+            w.bsum[2 * blockIdx.x + 1] = vg;
+        }
+    }
+}
+
 template <int G>
 __global__ void __launch_bounds__(1024) lc_prefix_kernel(int C, ListScanWork w) {
-    __shared__ int s_wp[32], s_wg[32], s_carry[2];
-    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
-    if (tid == 0) s_carry[0] = s_carry[1] = 0;
-    __syncthreads();
-    for (int base = 0; base < C; base += 4096) {
-        const int i0 = base + 4 * tid;
-        int c[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) c[j] = i0 + j < C ? w.pcnt[i0 + j] : 0;
-        int tp = 0, tg = 0;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            tp += c[j];
-            tg += (c[j] + G - 1) / G;
+    __shared__ int s_wp[32], s_wg[32], s_base[2];
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5, b = blockIdx.x;
+    if (wp == 0) {  // this block's base: the totals of the blocks before it
+        int bp = 0, bg = 0;
+        for (int j = lane; j < b; j += 32) {
+            bp += w.bsum[2 * j];
+            bg += w.bsum[2 * j + 1];
         }
-        int ip = tp, ig = tg;  // inclusive scan over the warp
+        bp = __reduce_add_sync(0xffffffffu, bp);
+        bg = __reduce_add_sync(0xffffffffu, bg);
+        if (lane == 0) {
+            s_base[0] = bp;
+            s_base[1] = bg;
+        }
+    }
+    const int i0 = b * LC_PFX + 4 * tid;
+    int c[4], tp, tg;
+    lc_prefix_load<G>(C, w, i0, c, tp, tg);
+    int ip = tp, ig = tg;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int vp = __shfl_up_sync(0xffffffffu, ip, o), vg = __shfl_up_sync(0xffffffffu, ig, o);
+        if (lane >= o) {
+            ip += vp;
+            ig += vg;
+        }
+    }
+    if (lane == 31) {
+        s_wp[wp] = ip;
+        s_wg[wp] = ig;
+    }
+    __syncthreads();
+    if (wp == 0) {  // exclusive scan of the 32 warp totals
+        const int vp = s_wp[lane], vg = s_wg[lane];
+        int jp = vp, jg = vg;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int vp = __shfl_up_sync(0xffffffffu, ip, o), vg = __shfl_up_sync(0xffffffffu, ig, o);
+            const int up = __shfl_up_sync(0xffffffffu, jp, o), ug = __shfl_up_sync(0xffffffffu, jg, o);
             if (lane >= o) {
-                ip += vp;
-                ig += vg;
+                jp += up;
+                jg += ug;
             }
         }
-        if (lane == 31) {
-            s_wp[wp] = ip;
-            s_wg[wp] = ig;
-        }
-        __syncthreads();
-        if (wp == 0) {  // exclusive scan of the 32 warp totals
-            const int vp = s_wp[lane], vg = s_wg[lane];
-            int jp = vp, jg = vg;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int up = __shfl_up_sync(0xffffffffu, jp, o), ug = __shfl_up_sync(0xffffffffu, jg, o);
-                if (lane >= o) {
-                    jp += up;
-                    jg += ug;
-                }
-            }
-            s_wp[lane] = jp - vp;
-            s_wg[lane] = jg - vg;
-        }
-        __syncthreads();
-        int rp = s_carry[0] + s_wp[wp] + ip - tp, rg = s_carry[1] + s_wg[wp] + ig - tg;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (i0 + j < C) {
-                w.pbeg[i0 + j] = rp;
-                w.fill[i0 + j] = rp;
-                w.gbeg[i0 + j] = rg;
-            }
-            rp += c[j];
-            rg += (c[j] + G - 1) / G;
-        }
-        __syncthreads();  // every thread has read the carry and the warp offsets
-        if (tid == 1023) {
-            s_carry[0] = rp;
-            s_carry[1] = rg;
-        }
-        __syncthreads();
+        s_wp[lane] = jp - vp;
+        s_wg[lane] = jg - vg;
     }
-    if (tid == 0) {
-        w.pbeg[C] = s_carry[0];
-        w.gbeg[C] = s_carry[1];
-        w.counters[0] = s_carry[1];
+    __syncthreads();
+    int rp = s_base[0] + s_wp[wp] + ip - tp, rg = s_base[1] + s_wg[wp] + ig - tg;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (i0 + j < C) {
+            w.pbeg[i0 + j] = rp;
+            w.fill[i0 + j] = rp;
+            w.gbeg[i0 + j] = rg;
+        }
+        rp += c[j];
+        rg += (c[j] + G - 1) / G;
+    }
+    if (b == gridDim.x - 1 && tid == 1023) {  // the totals
+        w.pbeg[C] = rp;
+        w.gbeg[C] = rg;
+        w.counters[0] = rg;
     }
 }
 
@@ -816,11 +847,7 @@ __global__ void __launch_bounds__(LC_SEL_NT) lc_select_kernel(DevIndex ix, ScanA
             }
         }
     }
-    for (int c = K + tid; c < stride; c += LC_SEL_NT) {
-        a.cand_key[o0 + c] = KEY_MAX;
-        a.cand_id[o0 + c] = -1;
-        if (ROWS_OUT) a.cand_list[o0 + c] = 0;
-    }
+    // (slots K .. stride - 1 stay unwritten: the finalize kernels read the first cand_cnt only)
     if (tid == 0) a.cand_cnt[q] = K;
 }
 
@@ -862,7 +889,10 @@ static cudaError_t launch_lc(const DevIndex& ix, const ScanArgs& a, const ListSc
     if ((e = rec(0)) != cudaSuccess) return e;
     if ((e = launch_scan_persistent(ix, pa, num_sms, 512, st, nullptr, false)) != cudaSuccess) return e;
     if ((e = rec(1)) != cudaSuccess) return e;
-    lc_prefix_kernel<G><<<1, 1024, 0, st>>>(C, w);
+    const int pblocks = (C + LC_PFX - 1) / LC_PFX;
+    lc_prefix_sums_kernel<G><<<pblocks, 1024, 0, st>>>(C, w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    lc_prefix_kernel<G><<<pblocks, 1024, 0, st>>>(C, w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     lc_fill_kernel<<<wblocks, 256, 0, st>>>(ix, a, w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
