@@ -615,7 +615,7 @@ __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
 // ivf_search.cpp:189-200). Bit-identical to the scan's exact table entries.
 template <int M>
 __device__ __forceinline__ float exact_adc(const DevIndex& ix, const float* xq, int l, int64_t row) {
-    constexpr int DS = 128 / M, H = M >= 8 ? M / 2 : M;  // sub-quantizers per batch of loads
+    constexpr int DS = 128 / M, H = M >= 8 ? M / 4 : M;  // sub-quantizers per batch of loads
     using CT = typename CodeRow<M>::T;
     const CT cr = load_row<M>(ix.codes + row * M);
     const uint32_t* cw = reinterpret_cast<const uint32_t*>(&cr);
@@ -863,6 +863,9 @@ int scan_persistent_stride(const ScanArgs& a) {
 // ---------------------------------------------------------------------------
 
 constexpr int RS_NT = 128;        // per-query kernels
+constexpr int RS_ORDER_NT = 256;  // the order kernel: its register sort holds RS_ORDER_NT * RS_ORDER_PER keys
+constexpr int RS_ORDER_PER = 4;
+static_assert(RS_ORDER_NT * RS_ORDER_PER >= 1024, "the final sort holds kl <= 1024 keys");
 constexpr int RS_CHUNK = 32;      // candidates per queue entry (one warp)
 
 // queue the chunks [i0, i1) of query q's list in round `round`
@@ -965,7 +968,7 @@ __global__ void __launch_bounds__(RS_NT) rs_first_kernel(DevIndex ix, ScanArgs a
 // one lane per listed candidate: its exact ADC distance (exact_adc: the reference's arithmetic, the
 // exact form's table entries bit for bit) keyed (distance, position) in place of its approximate key
 template <int M>
-__global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 4) rs_rescore_kernel(DevIndex ix, ScanArgs a, int round) {
+__global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 6) rs_rescore_kernel(DevIndex ix, ScanArgs a, int round) {
     const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * (RS_NT / 32);
     const int nch = min(a.rw.qcount[round], a.rw.qcap);
@@ -1029,9 +1032,9 @@ __global__ void __launch_bounds__(RS_NT) rs_second_kernel(DevIndex ix, ScanArgs 
 // its rank in its own set plus the number of smaller keys in the other; a large second set goes
 // through a radix select of the kk-th key and one sort instead. Then the results.
 template <int M>
-__global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a) {
+__global__ void __launch_bounds__(RS_ORDER_NT) rs_order_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
-    constexpr int META = RS_NT * FIN_SORT_PER;
+    constexpr int META = RS_ORDER_NT * RS_ORDER_PER;
     const int stride = a.cand_stride;
     u64* keys = reinterpret_cast<u64*>(fsm);                       // [stride] ordered keys, then scratch
     int32_t* ids = reinterpret_cast<int32_t*>(keys + stride);      // [stride] their hand-off slots
@@ -1048,27 +1051,27 @@ __global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a
     const int m0 = a.rw.cnt[2 * q], m = a.rw.cnt[2 * q + 1], m1 = m - m0;
     const int32_t* list = a.rw.list + hb;
     if (rr)
-        for (int x = tid; x < 128; x += RS_NT) xq[x] = a.queries[(int64_t)q * 128 + x];
+        for (int x = tid; x < 128; x += RS_ORDER_NT) xq[x] = a.queries[(int64_t)q * 128 + x];
     if (tid == 0) s_cnt2 = 0;
     int nout;
     if (m1 <= FIN_XTRA) {
-        for (int i = tid; i < m0; i += RS_NT) {
+        for (int i = tid; i < m0; i += RS_ORDER_NT) {
             const int c = list[i];
             sk[i] = a.cand_key[hb + c];
             ss[i] = c;
         }
-        for (int i = tid; i < m1; i += RS_NT) {
+        for (int i = tid; i < m1; i += RS_ORDER_NT) {
             const int c = list[m0 + i];
             xk[i] = a.cand_key[hb + c];
             xs[i] = c;
         }
         __syncthreads();
         if (m0 <= RANK_SORT_MAX) rank_sort(sk, ss, m0);
-        else block_sort_regs<RS_NT, FIN_SORT_PER>(sk, ss, m0);
+        else block_sort_regs<RS_ORDER_NT, RS_ORDER_PER>(sk, ss, m0);
         if (m1 > 1) rank_sort(xk, xs, m1);
         __syncthreads();
         nout = min(m, kk0);
-        for (int i = tid; i < m0; i += RS_NT) {
+        for (int i = tid; i < m0; i += RS_ORDER_NT) {
             const u64 key = sk[i];
             int lo = 0, hi = m1;  // smaller keys of the second set
             while (lo < hi) {
@@ -1081,7 +1084,7 @@ __global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a
                 ids[i + lo] = ss[i];
             }
         }
-        for (int i = tid; i < m1; i += RS_NT) {
+        for (int i = tid; i < m1; i += RS_ORDER_NT) {
             const u64 key = xk[i];
             int lo = 0, hi = m0;  // smaller keys of the first set
             while (lo < hi) {
@@ -1096,14 +1099,14 @@ __global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a
         }
     } else {
         // all m exact keys (m <= n <= stride) in keys[] / ids[], the kk0-th by a radix select
-        for (int i = tid; i < m; i += RS_NT) {
+        for (int i = tid; i < m; i += RS_ORDER_NT) {
             const int c = list[i];
             keys[i] = a.cand_key[hb + c];
             ids[i] = c;
         }
         __syncthreads();
         const u64 th2 = m > kk0 ? block_kth_flagged(keys, m, nullptr, kk0) : KEY_MAX;
-        for (int c0 = tid & ~31; c0 < m; c0 += RS_NT) {
+        for (int c0 = tid & ~31; c0 < m; c0 += RS_ORDER_NT) {
             const int c = c0 + lane;
             const bool in = c < m && keys[c] <= th2;
             const unsigned mk = __ballot_sync(0xffffffffu, in);
@@ -1119,14 +1122,14 @@ __global__ void __launch_bounds__(RS_NT) rs_order_kernel(DevIndex ix, ScanArgs a
         __syncthreads();
         nout = s_cnt2;  // min(m, kk0): the keys are unique
         if (nout <= RANK_SORT_MAX) rank_sort(sk, ss, nout);
-        else block_sort_regs<RS_NT, FIN_SORT_PER>(sk, ss, nout);
-        for (int c = tid; c < nout; c += RS_NT) {
+        else block_sort_regs<RS_ORDER_NT, RS_ORDER_PER>(sk, ss, nout);
+        for (int c = tid; c < nout; c += RS_ORDER_NT) {
             keys[c] = sk[c];
             ids[c] = ss[c];
         }
     }
     __syncthreads();
-    fin_output<M, RS_NT>(ix, a, q, hb, keys, ids, nout, xq, true);
+    fin_output<M, RS_ORDER_NT>(ix, a, q, hb, keys, ids, nout, xq, true);
 }
 
 template <int M>
@@ -1153,11 +1156,11 @@ static cudaError_t launch_rescore(const DevIndex& ix, const ScanArgs& a, cudaStr
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     rs_rescore_kernel<M><<<rgrid, RS_NT, 0, st>>>(ix, a, 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const size_t sm4 = (size_t)a.cand_stride * 12 + 512 + (size_t)(RS_NT * FIN_SORT_PER + FIN_XTRA) * 12;
+    const size_t sm4 = (size_t)a.cand_stride * 12 + 512 + (size_t)(RS_ORDER_NT * RS_ORDER_PER + FIN_XTRA) * 12;
     if (sm4 > 48 * 1024 &&
         (e = cudaFuncSetAttribute(rs_order_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4)) != cudaSuccess)
         return e;
-    rs_order_kernel<M><<<a.nq, RS_NT, sm4, st>>>(ix, a);
+    rs_order_kernel<M><<<a.nq, RS_ORDER_NT, sm4, st>>>(ix, a);
     return cudaGetLastError();
 }
 
