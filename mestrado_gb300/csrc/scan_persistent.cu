@@ -863,9 +863,9 @@ int scan_persistent_stride(const ScanArgs& a) {
 // ---------------------------------------------------------------------------
 
 constexpr int RS_NT = 128;        // per-query kernels
-constexpr int RS_ORDER_NT = 256;  // the order kernel: its register sort holds RS_ORDER_NT * RS_ORDER_PER keys
-constexpr int RS_ORDER_PER = 4;
-static_assert(RS_ORDER_NT * RS_ORDER_PER >= 1024, "the final sort holds kl <= 1024 keys");
+// the order kernel's threads and keys per thread of its register sort (1,024 keys): 256 x 4, or
+// 512 x 2 with the refinement re-rank, whose gathers want more loads in flight
+constexpr int RS_ORDER_KEYS = 1024;
 constexpr int RS_CHUNK = 32;      // candidates per queue entry (one warp)
 
 // queue the chunks [i0, i1) of query q's list in round `round`
@@ -1031,7 +1031,7 @@ __global__ void __launch_bounds__(RS_NT) rs_second_kernel(DevIndex ix, ScanArgs 
 // sorted in registers, the second (usually a few) by rank, the two merged -- each key's place is
 // its rank in its own set plus the number of smaller keys in the other; a large second set goes
 // through a radix select of the kk-th key and one sort instead. Then the results.
-template <int M>
+template <int M, int RS_ORDER_NT, int RS_ORDER_PER>
 __global__ void __launch_bounds__(RS_ORDER_NT) rs_order_kernel(DevIndex ix, ScanArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     constexpr int META = RS_ORDER_NT * RS_ORDER_PER;
@@ -1156,11 +1156,14 @@ static cudaError_t launch_rescore(const DevIndex& ix, const ScanArgs& a, cudaStr
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     rs_rescore_kernel<M><<<rgrid, RS_NT, 0, st>>>(ix, a, 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const size_t sm4 = (size_t)a.cand_stride * 12 + 512 + (size_t)(RS_ORDER_NT * RS_ORDER_PER + FIN_XTRA) * 12;
+    const size_t sm4 = (size_t)a.cand_stride * 12 + 512 + (size_t)(RS_ORDER_KEYS + FIN_XTRA) * 12;
+    const bool refine = a.flags & SCAN_REFINE;
+    void (*ord)(DevIndex, ScanArgs) = refine ? rs_order_kernel<M, 512, RS_ORDER_KEYS / 512>
+                                             : rs_order_kernel<M, 256, RS_ORDER_KEYS / 256>;
     if (sm4 > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(rs_order_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4)) != cudaSuccess)
+        (e = cudaFuncSetAttribute(ord, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4)) != cudaSuccess)
         return e;
-    rs_order_kernel<M><<<a.nq, RS_ORDER_NT, sm4, st>>>(ix, a);
+    ord<<<a.nq, refine ? 512 : 256, sm4, st>>>(ix, a);
     return cudaGetLastError();
 }
 
