@@ -1149,7 +1149,11 @@ static cudaError_t launch_rescore(const DevIndex& ix, const ScanArgs& a, cudaStr
     int dev = 0, sms = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    const int rgrid = sms * 4;  // persistent: the queues' lengths are known on the device only
+    // persistent, as many CTAs as fit: the queues' lengths are known on the device only
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rs_rescore_kernel<M>, RS_NT, 0)) != cudaSuccess)
+        return e;
+    const int rgrid = sms * std::max(per_sm, 1);
     rs_rescore_kernel<M><<<rgrid, RS_NT, 0, st>>>(ix, a, 0);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     rs_second_kernel<M><<<a.nq, RS_NT, 0, st>>>(ix, a);
