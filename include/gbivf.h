@@ -210,8 +210,8 @@ int gbivf_index_autotune(gbivf_index *ix, const float *d_queries, int nq, int k,
  * prints gettimeofday deltas (sequential/ivf_pq/ivf_search.cpp:105-111). */
 int gbivf_last_stage_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms);
 
-/* The same with the scan split in two: the scan kernel (tables, ADC, top-k)
- * and the finalize kernel (ordering, the precision form's exact re-score,
+/* The same with the scan split in two: the scan kernels (tables, ADC, top-k)
+ * and the finalize kernels (ordering, the precision form's exact re-score,
  * RERANK or the refinement re-rank). scan_ms + finalize_ms is the scan time
  * of gbivf_last_stage_ms. */
 int gbivf_last_stages_ms(gbivf_index *ix, float *coarse_ms, float *scan_ms, float *finalize_ms);

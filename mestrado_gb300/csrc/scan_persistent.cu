@@ -577,14 +577,12 @@ constexpr int FIN_NT = 128;
 // element, two barriers), larger ones by a bitonic network (log^2 barriers, fewer operations)
 constexpr int RANK_SORT_MAX = 256;
 constexpr int FIN_NT_BIG = 512;
-// the precision form's error bound (finalize_kernel): relative, then absolute per unit of
+// the precision form's error bound (rs_second_kernel): relative, then absolute per unit of
 // ||r||^2 + sum_s max_c ||c_s||^2, then absolute (FP16 subnormals)
 constexpr double MIX_DELTA = 0x1p-9;
 constexpr double MIX_EPS_REL = 0x1p-12;
 constexpr double MIX_EPS_ABS = 0x1p-12;
-// the precision form's final sort: keys per thread of the register bitonic network, and the
-// largest second re-score round merged without a second select
-constexpr int FIN_SORT_PER = 8;
+// the largest second re-score round that the order kernel merges without a second select
 constexpr int FIN_XTRA = 256;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
