@@ -11,7 +11,9 @@ each query with its own nprobe (log-uniform in 1..256) and k (from
 * plain: FP32 throughout, the reference's arithmetic (the drop-in);
 * mixed: BF16 tensor-core coarse stage with an FP32 re-check of every
   centroid within the error margin (the same probe lists), FP16 PQ tables
-  summed in FP32 with the 4k best re-scored exactly (the same ids).
+  summed in FP32, the candidates within the tables' error bound re-scored
+  exactly (the same ids on every query the engine proves; the count of the
+  others is reported as ``unproven_queries``).
 
 A step is one search of the whole batch, replayed as a CUDA graph.
 
@@ -22,16 +24,18 @@ A step is one search of the whole batch, replayed as a CUDA graph.
 * ``e2e``: the same batch through the host C ABI (gbivf_search_batched):
   queries, nprobe and k copied from pinned host memory, ids and distances
   copied back, per step.
-* ``roofline``: the dominant kernel of the mixed step (the ADC scan):
-  algorithmic bytes (sum over queries of the probed lists' codes, n_l * m)
-  over its CUDA-event time, against the measured HBM copy bandwidth.
+* ``roofline``: the dominant kernel of the mixed step (the list-centric ADC
+  scan): algorithmic bytes (sum over queries of the codes of the probes it
+  scans, n_l * m) over its CUDA-event time, against the measured HBM copy
+  bandwidth; ``traffic`` from the committed ncu summary.
 * ``cpu_baseline``: the CPU oracle (the plain-C restatement of the
   reference's search) on all host cores, on a sample of the same queries.
 * ``parity``: the plain form against the oracle on a sample of queries (ids
   and distance bits), the mixed form against the plain form on all queries.
 * ``sub``: the 1M drop-in workload (``ivfpq_search`` with re-rank, all
   10,000 queries checked against the oracle, the reference's OpenMP
-  ``core_cpu`` timed) and the 10M workload (C = 65,536, w = 32, k = 100).
+  ``core_cpu`` timed), the 10M workload (C = 65,536, w = 32, k = 100) and
+  the 1B workload (refinement re-rank).
 
 ``--impl reference`` times the oracle alone on the headline workload, in
 steps of a bounded sample of its queries, with every host thread. The index

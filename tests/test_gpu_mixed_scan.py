@@ -94,7 +94,7 @@ def test_mixed_scan_on_gpu_built_zipf_index():
 
 def test_unproven_count_follows_the_last_search():
     """gbivf_last_unproven: 0 after an exact-form search; after a precision-form search with an
-    approximate selection of alpha * k, a count between 0 and the number of queries."""
+    approximate selection of max(alpha * k, k + 64), a count between 0 and the number of queries."""
     from mestrado_gb300.engine import GpuIndex
 
     g = golden_cases.load("m16")
