@@ -88,17 +88,30 @@ __device__ __forceinline__ void pg_chunk(const PgArgs& p, const uint32_t (&r)[32
     if (MODE == PG_FILTER) {
         // gs holds t_c = G_c - qlen_w K_c with qlen_w >= this row's ||q|| (the warp's largest), so
         // acc - t_c >= h is implied by the row's exact candidate test; survivors (rare) go to this
-        // thread's region with plain stores, the exact tests run in the candidate kernel
+        // thread's region with plain stores, the exact tests run in the candidate kernel. The 32
+        // columns are first reduced to their largest acc - t_c (a subtract and a max per pair), and
+        // only a chunk holding a survivor is tested pair by pair.
+        float mx = -__int_as_float(0x7f800000);
 #pragma unroll
         for (int q4 = 0; q4 < 8; q4++) {
             const float4 t = reinterpret_cast<const float4*>(gs)[q4];
-            const float tv[4] = {t.x, t.y, t.z, t.w};
+            mx = fmaxf(mx, __uint_as_float(r[4 * q4 + 0]) - t.x);
+            mx = fmaxf(mx, __uint_as_float(r[4 * q4 + 1]) - t.y);
+            mx = fmaxf(mx, __uint_as_float(r[4 * q4 + 2]) - t.z);
+            mx = fmaxf(mx, __uint_as_float(r[4 * q4 + 3]) - t.w);
+        }
+        if (mx >= h) {
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const float acc = __uint_as_float(r[4 * q4 + e]);
-                if (acc - tv[e] >= h) {
-                    sv[min(nsv, p.f.sreg - 1)] = make_int2(c0 + 4 * q4 + e, (int)r[4 * q4 + e]);
-                    nsv++;
+            for (int q4 = 0; q4 < 8; q4++) {
+                const float4 t = reinterpret_cast<const float4*>(gs)[q4];
+                const float tv[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float acc = __uint_as_float(r[4 * q4 + e]);
+                    if (acc - tv[e] >= h) {
+                        sv[min(nsv, p.f.sreg - 1)] = make_int2(c0 + 4 * q4 + e, (int)r[4 * q4 + e]);
+                        nsv++;
+                    }
                 }
             }
         }
