@@ -47,6 +47,14 @@ def test_invalid_arguments_return_status():
     assert rc == 4 and b"ks" in lib.gbivf_last_error()  # ks > 256 unsupported
     assert lib.gbivf_ivfpq_search(None, None, 1, 1, 1, 1, 0, None, None) == 1
     assert lib.gbivf_index_destroy(None) == 0
+    # the reporting entry points of the batched engine
+    n = C.c_int64()
+    assert lib.gbivf_last_unproven(None, C.byref(n)) == 1
+    assert lib.gbivf_last_scan_parts(None, None, None) == 1
+    k = C.c_int()
+    assert lib.gbivf_graph_kernel_count(None, C.byref(k)) == 1
+    assert lib.gbivf_index_scan_form(None, C.byref(k), C.byref(k)) == 1
+    assert lib.gbivf_last_stages_ms(None, None, None, None) == 1
 
 
 def test_codes_out_of_range_rejected():
