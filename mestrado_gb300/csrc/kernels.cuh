@@ -44,14 +44,14 @@ struct DevIndex {
 // The precision form's exact re-score (scan_persistent.cu, launch_finalize): per-query selects and
 // gathers around a flat re-score kernel that works through queues of 32-candidate chunks.
 struct RescoreWork {
-    int32_t* list = nullptr;            // nq x cand_stride: hand-off slots to re-score, first round then second
-    int* cnt = nullptr;                 // nq x 2: list length after the first round, after the second
-    unsigned* marks = nullptr;          // nq x cand_stride / 32: slots of the first round
-    unsigned long long* t0 = nullptr;   // nq: largest exact key of the first round
+    int32_t* list = nullptr;            // nq x cand_stride: hand-off slots to re-score, first set then second
+    int* cnt = nullptr;                 // nq x 2: list length after the first set, after the second
+    unsigned* marks = nullptr;          // nq x cand_stride / 32: slots of the first set
+    unsigned long long* t0 = nullptr;   // nq: largest exact key of the first set
     unsigned long long* amax = nullptr; // nq: largest approximate key of the hand-off
     float* r2 = nullptr;                // nq: largest squared residual norm over the query's probes
-    int4* queue = nullptr;              // 2 x qcap chunks (query, first, end, 0), one queue per round
-    int* qcount = nullptr;              // [0], [1]: chunks queued per round
+    int4* queue = nullptr;              // 2 x qcap chunks (query, first, end, 0), one queue per set
+    int* qcount = nullptr;              // [0], [1]: chunks queued per set
     int qcap = 0;
 };
 
@@ -139,7 +139,7 @@ cudaError_t launch_finalize(const DevIndex& ix, const ScanArgs& a, cudaStream_t 
 bool scan_persistent_supported(const DevIndex& ix, const ScanArgs& a);
 // candidate slots per query the persistent scan needs in ScanArgs::cand_*
 int scan_persistent_stride(const ScanArgs& a);
-// chunks per round of the precision form's re-score queue for nq queries and a hand-off stride
+// chunks per set of the precision form's re-score queue for nq queries and a hand-off stride
 int rescore_queue_cap(int nq, int stride);
 
 // List-centric scan (scan_lists.cu): the (query, list) pairs of a batch grouped by list, G queries

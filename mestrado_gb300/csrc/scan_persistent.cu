@@ -582,7 +582,7 @@ constexpr int FIN_NT_BIG = 512;
 constexpr double MIX_DELTA = 0x1p-9;
 constexpr double MIX_EPS_REL = 0x1p-12;
 constexpr double MIX_EPS_ABS = 0x1p-12;
-// the largest second re-score round that the order kernel merges without a second select
+// the largest second re-score set that the order kernel merges without a second select
 constexpr int FIN_XTRA = 256;
 
 __device__ inline void bitonic_sort_pairs(u64* a, int32_t* b, int n) {
@@ -849,12 +849,12 @@ int scan_persistent_stride(const ScanArgs& a) {
 // candidates, no candidate with A >= tau = (T0 + eps_q) / (1 - MIX_DELTA) can enter the exact
 // top-kk: the kk best and those below tau are re-scored, no other. Five launches:
 //   rs_first_kernel   per query: the kk-th approximate key (radix select), the kk best listed
-//                     (round 1), the residual bound r2;
+//                     (the first set), the residual bound r2;
 //   rs_rescore_kernel flat: one lane per listed candidate, 32-candidate chunks from a queue; the
 //                     exact key replaces the approximate one in the hand-off; T0 by atomicMax;
-//   rs_second_kernel  per query: tau, the other candidates below it listed (round 2), the proof;
-//   rs_rescore_kernel round 2;
-//   rs_order_kernel   per query: the two rounds sorted (registers / by rank) and merged, then the
+//   rs_second_kernel  per query: tau, the other candidates below it listed (the second set), the proof;
+//   rs_rescore_kernel on the second set;
+//   rs_order_kernel   per query: the two sets sorted (registers / by rank) and merged, then the
 //                     results written (or re-ranked) by fin_output.
 // Only the re-score kernel holds the exact arithmetic's registers; the per-query kernels run at
 // the occupancy their shared memory allows.
@@ -866,15 +866,15 @@ constexpr int RS_NT = 128;        // per-query kernels
 constexpr int RS_ORDER_KEYS = 1024;
 constexpr int RS_CHUNK = 32;      // candidates per queue entry (one warp)
 
-// queue the chunks [i0, i1) of query q's list in round `round`
-__device__ __forceinline__ void rs_enqueue(const ScanArgs& a, int round, int q, int i0, int i1) {
+// queue the chunks [i0, i1) of query q's list in the queue of set `set` (0: first, 1: second)
+__device__ __forceinline__ void rs_enqueue(const ScanArgs& a, int set, int q, int i0, int i1) {
     const int nch = (i1 - i0 + RS_CHUNK - 1) / RS_CHUNK;
     __shared__ int s_base;
-    if (threadIdx.x == 0) s_base = nch > 0 ? atomicAdd(a.rw.qcount + round, nch) : 0;
+    if (threadIdx.x == 0) s_base = nch > 0 ? atomicAdd(a.rw.qcount + set, nch) : 0;
     __syncthreads();
     for (int j = threadIdx.x; j < nch; j += blockDim.x) {
         const int slot = s_base + j;
-        if (slot < a.rw.qcap) a.rw.queue[(int64_t)round * a.rw.qcap + slot] = make_int4(q, i0 + j * RS_CHUNK, i1, 0);
+        if (slot < a.rw.qcap) a.rw.queue[(int64_t)set * a.rw.qcap + slot] = make_int4(q, i0 + j * RS_CHUNK, i1, 0);
     }
 }
 
@@ -966,11 +966,11 @@ __global__ void __launch_bounds__(RS_NT) rs_first_kernel(DevIndex ix, ScanArgs a
 // one lane per listed candidate: its exact ADC distance (exact_adc: the reference's arithmetic, the
 // exact form's table entries bit for bit) keyed (distance, position) in place of its approximate key
 template <int M>
-__global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 6) rs_rescore_kernel(DevIndex ix, ScanArgs a, int round) {
+__global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 6) rs_rescore_kernel(DevIndex ix, ScanArgs a, int set) {
     const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * (RS_NT / 32);
-    const int nch = min(a.rw.qcount[round], a.rw.qcap);
-    const int4* queue = a.rw.queue + (int64_t)round * a.rw.qcap;
+    const int nch = min(a.rw.qcount[set], a.rw.qcap);
+    const int4* queue = a.rw.queue + (int64_t)set * a.rw.qcap;
     for (int ch = blockIdx.x * (RS_NT / 32) + (threadIdx.x >> 5); ch < nch; ch += nwarps) {
         const int4 e = queue[ch];  // (query, first, end, 0)
         const int q = e.x, i = e.y + lane;
@@ -982,7 +982,7 @@ __global__ void __launch_bounds__(RS_NT, M == 4 ? 2 : 6) rs_rescore_kernel(DevIn
                            key_payload(a.cand_key[hb + c]));
             a.cand_key[hb + c] = key;
         }
-        if (round == 0) {
+        if (set == 0) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const u64 x = __shfl_xor_sync(0xffffffffu, key, o);
@@ -1025,7 +1025,7 @@ __global__ void __launch_bounds__(RS_NT) rs_second_kernel(DevIndex ix, ScanArgs 
     rs_enqueue(a, 1, q, m0, m);
 }
 
-// The kk best exact keys of the re-scored set, in order: the first round's set (min(n, kk) keys)
+// The kk best exact keys of the re-scored set, in order: the first set (min(n, kk) keys)
 // sorted in registers, the second (usually a few) by rank, the two merged -- each key's place is
 // its rank in its own set plus the number of smaller keys in the other; a large second set goes
 // through a radix select of the kk-th key and one sort instead. Then the results.
@@ -1169,7 +1169,7 @@ static cudaError_t launch_rescore(const DevIndex& ix, const ScanArgs& a, cudaStr
     return cudaGetLastError();
 }
 
-// the re-score workspace's queue capacity for a batch (chunks of both rounds, per round)
+// the re-score workspace's queue capacity for a batch (chunks of either set, per set)
 int rescore_queue_cap(int nq, int stride) { return nq * (stride / RS_CHUNK + 1); }
 
 template <int M, bool MIXED>
