@@ -1177,7 +1177,7 @@ def main():
                     help="large workloads: queries checked against the oracle")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
-    ap.add_argument("--no-sub", action="store_true", help="headline: skip the drop-in and 10M sub-records")
+    ap.add_argument("--no-sub", action="store_true", help="headline: skip the drop-in, 10M and 1B sub-records")
     ap.add_argument("--profile-steps", action="store_true",
                     help="large workloads: mark the mixed form's timed steps for a profiler started with "
                          "--profile-from-start off (numbers printed under a profiler are not measurements)")
